@@ -1,0 +1,346 @@
+#!/usr/bin/env python3
+"""Benchmark of the phase-space hot path on the N=5 D0 workload (2^24 events).
+
+Workload (one "step"): mother M = 1.86484 GeV at rest -> K (0.493677) + 4 pi (0.13957),
+Philox2x64-7, seed 0x3039, 2^24 events:
+  * store path: Generate into Decays columns (5 x Vector4R) + generation-time weight +
+    Decays::Unweight hit-or-miss flags  (32*5 + 8 + 1 = 169 bytes written per event);
+  * storage-free AverageOn of |BW(m(K pi1))|^2, mass 0.8955 GeV, width 0.0473 GeV.
+value = events of the step / step time (events/s).  Outputs written per step (2.84 GB)
+exceed the 129 MB L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference] [--precision fp64]
+
+--impl reference times the reference algorithm on the host cores (the oracle port of
+Hydra's cpp/omp path, all threads) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO))
+
+N_DAUGHTERS = 5
+MOTHER = 1.86484
+MASSES = [0.493677, 0.13957, 0.13957, 0.13957, 0.13957]
+SEED = 0x3039
+BW = (0, 1, 0.8955, 0.0473)
+UNWEIGHT_SEED = 0x180EC6D33CFD0ABA
+BYTES_PER_EVENT = 32 * N_DAUGHTERS + 8 + 1
+METRIC = "events/s (N=5 phase-space Generate+weights+unweight flags, then AverageOn |BW|^2)"
+
+
+def workload_config(n, precision):
+    return {"workload": "D0 -> K pi pi pi pi phase space: Generate (5 Vector4R + weight + unweight flag) "
+                        "+ AverageOn |BW(m_K_pi1)|^2",
+            "n_events": n, "n_daughters": N_DAUGHTERS, "mother_mass": MOTHER, "engine": "philox2x64-7",
+            "seed": SEED, "precision": precision, "bytes_per_event_stored": BYTES_PER_EVENT,
+            "l2": "outputs per step (%.2f GB) exceed L2; no flush" % (n * BYTES_PER_EVENT / 1e9)}
+
+
+def measured_peak_hbm():
+    p = REPO / "MEASURED_PEAKS.json"
+    try:
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(precision):
+    """DRAM bytes per launch of the store kernel from the committed ncu summary, if any."""
+    p = REPO / "profiles" / "traffic.json"
+    try:
+        d = json.loads(p.read_text())
+        return d.get(f"generate_n5_{precision}")
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.proc = None
+        self.lines = []
+        self.device_index = device_index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device_index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "gpu" else "gloo"
+        dist.init_process_group(backend=backend)
+    return world, rank
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ------------------------------------------------------------------------------ CPU baseline
+
+def cpu_sample(seconds=3.0, n_sample=1 << 21, nthreads=0):
+    """Oracle port of the reference (FP64, -O3, OpenMP over all host threads): store step +
+    AverageOn on chunks of the workload until `seconds` of wall time have elapsed."""
+    import numpy as np
+    from oracle import oracle as O
+    O.build()
+    ch = O.make_channel(MASSES, MOTHER, SEED, O.ENGINE_PHILOX)
+    fn = O.make_functor(2, *BW)
+    four = np.empty((N_DAUGHTERS, n_sample, 4))
+    w = np.empty(n_sample)
+    fl = np.empty(n_sample, dtype=np.uint8)
+    O.store_step(ch, 0, 4096, UNWEIGHT_SEED, four[:, :4096].copy(), w[:4096].copy(), fl[:4096].copy(), nthreads)
+    t0 = time.perf_counter()
+    done, first = 0, 0
+    while True:
+        O.store_step(ch, first, n_sample, UNWEIGHT_SEED, four, w, fl, nthreads)
+        O.average_on(ch, fn, first, n_sample, nthreads=nthreads if nthreads else 0)
+        done += n_sample
+        first += n_sample
+        if time.perf_counter() - t0 >= seconds:
+            break
+    dt = time.perf_counter() - t0
+    cores = nthreads if nthreads > 0 else O.max_threads()
+    return done / dt, cores, f"{done} events ({done // n_sample} chunks of {n_sample}), {dt:.2f} s wall"
+
+
+def run_reference(args):
+    world, rank = dist_setup(args)
+    if rank != 0:
+        return 0
+    rate, cores, sample = cpu_sample(seconds=max(1.0, 1.5 * args.steps / 10))
+    vals = []
+    for _ in range(args.warmup):
+        cpu_sample(seconds=0.2)
+    for _ in range(args.steps):
+        r, _, _ = cpu_sample(seconds=1.0)
+        vals.append(r)
+    value = statistics.median(vals)
+    n = args.n
+    line = {
+        "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * n / value, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded counter-based RNG)",
+        "config": workload_config(n, "fp64"), "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": "events/s", "cores": cores, "kind": "port",
+                         "sample": f"per step: {sample}; oracle port of Hydra's omp path (reference not "
+                                   "buildable on the GPU host: its sources are absent there)"},
+        "e2e": {"value": value, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------------------ GPU arm
+
+def run_gpu(args):
+    import torch
+    world, rank = dist_setup(args)
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    from hydra_gb300 import api
+    import hydra_gb300
+    hydra_gb300.lib()          # raises if the CUDA library is missing: no fallback
+
+    n = args.n
+    first = rank * n           # weak scaling: each rank owns its own event range
+    ch = api.make_channel(MASSES, MOTHER, SEED, "philox")
+    fn = api.functor_bw2(*BW)
+    dev = torch.device("cuda", local)
+    four = torch.empty((N_DAUGHTERS, n, 4), dtype=torch.float64, device=dev)
+    w = torch.empty(n, dtype=torch.float64, device=dev)
+    fl = torch.empty(n, dtype=torch.uint8, device=dev)
+    stats = torch.zeros(3, dtype=torch.float64, device=dev)
+    ws = torch.empty(api.average_on_workspace_size(n) // 8, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def step(ev=None):
+        if ev is not None:
+            ev[0].record(stream)
+        api.generate(ch, first, four, w, fl, UNWEIGHT_SEED, args.precision, stream)
+        if ev is not None:
+            ev[1].record(stream)
+        api.average_on(ch, first, n, fn, stats, ws, args.precision, stream)
+        if ev is not None:
+            ev[2].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    with ClockSampler(local) as clocks:
+        barrier(world)
+        torch.cuda.synchronize()
+        t_start = torch.cuda.Event(enable_timing=True)
+        t_end = torch.cuda.Event(enable_timing=True)
+        t_start.record(stream)
+        for k in range(args.steps):
+            step(evs[k])
+        t_end.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+    total_ms = t_start.elapsed_time(t_end)
+    gen_ms = [e[0].elapsed_time(e[1]) for e in evs]
+    avg_ms = [e[1].elapsed_time(e[2]) for e in evs]
+    total_ms = max_over_ranks(total_ms, world)
+    ms_per_step = total_ms / args.steps
+    value = world * n / (ms_per_step / 1e3)
+
+    # end to end through the host-output entry point: Decays land in pinned host memory,
+    # the AverageOn result is read back; copies are inside the timed region.
+    e2e = None
+    if not args.no_e2e:
+        hfour = torch.empty((N_DAUGHTERS, n, 4), dtype=torch.float64).pin_memory()
+        hw = torch.empty(n, dtype=torch.float64).pin_memory()
+        hfl = torch.empty(n, dtype=torch.uint8).pin_memory()
+        hstats = torch.zeros(3, dtype=torch.float64).pin_memory()
+
+        def e2e_step():
+            api.generate_host(ch, first, hfour, hw, hfl, UNWEIGHT_SEED, args.precision, 0, stream)
+            api.average_on(ch, first, n, fn, stats, ws, args.precision, stream)
+            hstats.copy_(stats, non_blocking=True)
+            stream.synchronize()
+
+        for _ in range(max(1, min(args.warmup, 2))):
+            e2e_step()
+        e2e_steps = max(2, min(args.steps, 5))
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_step()
+        barrier(world)
+        dt = max_over_ranks(time.perf_counter() - t0, world)
+        e2e = {"value": world * n * e2e_steps / dt, "unit": "events/s", "h2d_bytes_per_step": 0,
+               "d2h_bytes_per_step": n * BYTES_PER_EVENT + 24, "steps": e2e_steps,
+               "note": "hps_generate_host into pinned host Decays + AverageOn result read back"}
+
+    peak, peak_kind = measured_peak_hbm()
+    gen_avg_s = statistics.mean(gen_ms) / 1e3
+    achieved = n * BYTES_PER_EVENT / gen_avg_s / 1e9
+    traffic = profiled_traffic(args.precision)
+    roofline = {"bound": "hbm", "kernel": "k_generate (store path)", "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                "traffic": traffic, "algorithmic_bytes_per_launch": n * BYTES_PER_EVENT,
+                "kernel_ms": statistics.mean(gen_ms)}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        rate, cores, sample = cpu_sample(seconds=3.0)
+        cpu = {"value": rate, "unit": "events/s", "cores": cores, "kind": "port", "sample": sample}
+
+    csum = clocks.summary()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64fix",
+            "data": "synthetic (seeded counter-based RNG; no dataset)",
+            "config": workload_config(n, args.precision) | {"parallelism": f"replicas{world}"},
+            "parts": {"generate_ms": statistics.mean(gen_ms), "average_on_ms": statistics.mean(avg_ms),
+                      "generate_events_per_s": n / gen_avg_s,
+                      "average_on_events_per_s": n / (statistics.mean(avg_ms) / 1e3)},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": 3 * args.steps, "clocks": csum,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
+    ap.add_argument("--precision", choices=["fp64", "fp32_fix"], default="fp64")
+    ap.add_argument("--n", type=int, default=1 << 24)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,120 @@
+"""hydra_gb300 -- GB300-native phase-space generator (Hydra's PhaseSpace hot path).
+
+Python binding of the C ABI in ``include/hps.h`` (``libhps.so``, hand-written sm_103a
+kernels).  PyTorch provides device memory and streams; every computation runs in
+``libhps.so``.  There is no CPU fallback: if the library is missing, loading raises.
+
+Host-side mirror of the reference API for this path (hydra/PhaseSpace.h:86-346):
+
+    ps = PhaseSpace(5.27934, [3.0969, 0.493677, 0.13957], engine="philox")
+    ps.SetSeed(0x3039)
+    events = ps.Generate(mother, n)          # Decays: N columns of Vector4R (+ weights)
+    mean, err = ps.AverageOn(mother, functor, n)
+    w, fvals = ps.Evaluate(mother, n, functor, ...)
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+from .build import LIB as _LIB_PATH
+
+HPS_MAX_DAUGHTERS = 10
+HPS_AVG_TILE = 4096
+
+OK, ERR_BAD_ARG, ERR_NO_ENERGY, ERR_OOM, ERR_BUDGET, ERR_TIMEOUT, ERR_CUDA, ERR_UNSUPPORTED = range(8)
+ENGINE_PHILOX, ENGINE_SQUARES3 = 0, 1
+PREC_FP64, PREC_FP32_FIX = 0, 1
+FN_ONE, FN_MASS2, FN_BW2 = 0, 1, 2
+DEFAULT_UNWEIGHT_SEED = 0x180EC6D33CFD0ABA   # hydra/Decays.h:253
+
+
+class HpsChannel(ctypes.Structure):
+    _fields_ = [
+        ("n_daughters", ctypes.c_int32),
+        ("engine", ctypes.c_int32),
+        ("seed", ctypes.c_uint64),
+        ("ecm", ctypes.c_double),
+        ("max_weight", ctypes.c_double),
+        ("beta", ctypes.c_double * 3),
+        ("masses", ctypes.c_double * HPS_MAX_DAUGHTERS),
+    ]
+
+
+class HpsFunctor(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int32),
+        ("i", ctypes.c_int32),
+        ("j", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("a", ctypes.c_double),
+        ("b", ctypes.c_double),
+    ]
+
+
+class HpsStats(ctypes.Structure):
+    _fields_ = [("mean", ctypes.c_double), ("m2", ctypes.c_double), ("w", ctypes.c_double)]
+
+
+class HpsError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"hps status {status}: {message}")
+        self.status = status
+
+
+# Exported symbols and their ctypes signatures; tests check this list against include/hps.h.
+_vp, _u64, _i32, _dbl, _sz = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32, ctypes.c_double, ctypes.c_size_t
+SIGNATURES = {
+    "hps_channel_init": (_i32, [ctypes.POINTER(HpsChannel), _i32, _i32, _u64, _dbl, _vp, _vp]),
+    "hps_generate": (_i32, [ctypes.POINTER(HpsChannel), _u64, _u64, _vp, _vp, _vp, _u64, _i32, _vp]),
+    "hps_generate_host": (_i32, [ctypes.POINTER(HpsChannel), _u64, _u64, _vp, _vp, _vp, _u64, _i32, _u64,
+                                 _vp]),
+    "hps_evaluate": (_i32, [ctypes.POINTER(HpsChannel), _u64, _u64, _vp, _i32, _vp, _vp, _i32, _vp]),
+    "hps_average_on_workspace_size": (_sz, [_u64]),
+    "hps_average_on": (_i32, [ctypes.POINTER(HpsChannel), _u64, _u64, ctypes.POINTER(HpsFunctor), _vp, _vp,
+                              _sz, _i32, _vp]),
+    "hps_event_weights": (_i32, [_i32, _vp, _dbl, _u64, _vp, _vp, _vp]),
+    "hps_unweight_flags": (_i32, [_i32, _vp, _dbl, _u64, _vp, _u64, _u64, _vp, _vp]),
+    "hps_rng_words": (_i32, [_i32, _i32, _u64, _u64, _u64, _vp, _vp]),
+    "hps_default_seed": (_u64, [_i32, _vp]),
+    "hps_last_error": (ctypes.c_char_p, []),
+    "hps_abi_version": (_i32, []),
+}
+
+_lib = None
+
+
+def library_path() -> Path:
+    return Path(os.environ.get("HPS_LIBRARY", str(_LIB_PATH)))
+
+
+def lib():
+    """Loads libhps.so (raises if it has not been built: there is no fallback)."""
+    global _lib
+    if _lib is None:
+        path = library_path()
+        if not path.exists():
+            raise RuntimeError(f"libhps.so not found at {path}; build it with `python -m hydra_gb300.build`")
+        L = ctypes.CDLL(str(path))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status: int) -> None:
+    if status != OK:
+        raise HpsError(status, lib().hps_last_error().decode(errors="replace"))
+
+
+from .api import (  # noqa: E402
+    Channel, Decays, PhaseSpace, Vector4R, functor_bw2, functor_mass2, functor_one, make_channel,
+)
+
+__all__ = [
+    "lib", "check", "HpsError", "HpsChannel", "HpsFunctor", "HpsStats", "Channel", "Decays", "PhaseSpace",
+    "Vector4R", "make_channel", "functor_one", "functor_mass2", "functor_bw2",
+]

@@ -1,0 +1,346 @@
+"""Host-side mirror of Hydra's phase-space interface over the C ABI.
+
+Names, argument meaning and error behaviour follow the reference:
+  hydra::PhaseSpace<N,GRND>   hydra/PhaseSpace.h:86-346, hydra/detail/PhaseSpace.inl
+  hydra::Decays<tuple<P...>>  hydra/Decays.h:67-651, hydra/detail/Decays.inl
+  hydra::Vector4R             hydra/Vector4R.h:59-138
+Device memory and streams come from PyTorch; every computation is a libhps.so call.
+
+The low-level functions (generate, evaluate, average_on, ...) take torch CUDA tensors
+and launch on the current torch stream (or an explicit one) without synchronising.
+The class methods synchronise like the reference's blocking Thrust calls.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from dataclasses import dataclass
+from typing import Iterable, Sequence
+
+import torch
+
+from . import (
+    DEFAULT_UNWEIGHT_SEED, ENGINE_PHILOX, ENGINE_SQUARES3, ERR_BAD_ARG, ERR_NO_ENERGY, FN_BW2, FN_MASS2, FN_ONE,
+    HPS_MAX_DAUGHTERS, PREC_FP32_FIX, PREC_FP64, HpsChannel, HpsError, HpsFunctor, check, lib,
+)
+
+_ENGINES = {"philox": ENGINE_PHILOX, "squares3": ENGINE_SQUARES3, "default": ENGINE_SQUARES3,
+            ENGINE_PHILOX: ENGINE_PHILOX, ENGINE_SQUARES3: ENGINE_SQUARES3}
+_PRECISIONS = {"fp64": PREC_FP64, "fp32_fix": PREC_FP32_FIX, PREC_FP64: PREC_FP64, PREC_FP32_FIX: PREC_FP32_FIX}
+
+Channel = HpsChannel
+
+
+def _stream_handle(stream) -> ctypes.c_void_p:
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    if isinstance(stream, torch.cuda.Stream):
+        return ctypes.c_void_p(stream.cuda_stream)
+    return ctypes.c_void_p(int(stream))
+
+
+def _dptr(t: torch.Tensor | None) -> ctypes.c_void_p:
+    if t is None:
+        return ctypes.c_void_p(0)
+    if not t.is_cuda:
+        raise ValueError("expected a CUDA tensor")
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _double_array(values: Sequence[float]):
+    arr = (ctypes.c_double * max(1, len(values)))()
+    for i, v in enumerate(values):
+        arr[i] = float(v)
+    return arr
+
+
+def _ptr_array(tensors: Sequence[torch.Tensor]):
+    arr = (ctypes.c_void_p * max(1, len(tensors)))()
+    for i, t in enumerate(tensors):
+        arr[i] = _dptr(t).value
+    return arr
+
+
+# ----------------------------------------------------------------------------- functors
+
+def functor_one() -> HpsFunctor:
+    return HpsFunctor(FN_ONE, 0, 1, 0, 0.0, 0.0)
+
+
+def functor_mass2(i: int, j: int) -> HpsFunctor:
+    """f = mass2(p_i + p_j)."""
+    return HpsFunctor(FN_MASS2, i, j, 0, 0.0, 0.0)
+
+
+def functor_bw2(i: int, j: int, mass: float, width: float) -> HpsFunctor:
+    """f = 1 / ((mass^2 - mass2(p_i+p_j))^2 + (mass*width)^2), |relativistic BW|^2."""
+    return HpsFunctor(FN_BW2, i, j, 0, float(mass), float(width))
+
+
+# ----------------------------------------------------------------------------- channel
+
+def make_channel(masses: Sequence[float], mother_mass: float, seed: int, engine="philox",
+                 mother: Sequence[float] | None = None) -> HpsChannel:
+    """Channel scalars as hydra::PhaseSpace's constructor computes them (PhaseSpace.inl:42-90).
+
+    Raises ValueError (std::invalid_argument) for a mass <= 0 and RuntimeError
+    (std::runtime_error) when M - sum(m) <= 0."""
+    ch = HpsChannel()
+    m = _double_array(masses)
+    mom = _double_array(mother if mother is not None else [mother_mass, 0.0, 0.0, 0.0])
+    st = lib().hps_channel_init(ctypes.byref(ch), len(masses), _ENGINES[engine], int(seed) & (2**64 - 1),
+                                float(mother_mass), ctypes.cast(m, ctypes.c_void_p),
+                                ctypes.cast(mom, ctypes.c_void_p))
+    if st == ERR_BAD_ARG:
+        raise ValueError(lib().hps_last_error().decode())
+    if st == ERR_NO_ENERGY:
+        raise RuntimeError(lib().hps_last_error().decode())
+    check(st)
+    return ch
+
+
+def default_seed(masses: Sequence[float]) -> int:
+    m = _double_array(masses)
+    return int(lib().hps_default_seed(len(masses), ctypes.cast(m, ctypes.c_void_p)))
+
+
+# ----------------------------------------------------------------------------- raw launches
+
+def generate(ch: HpsChannel, first: int, four: torch.Tensor | Sequence[torch.Tensor], weights=None, flags=None,
+             unweight_seed: int = DEFAULT_UNWEIGHT_SEED, precision="fp64", stream=None) -> None:
+    """four: [N, n, 4] float64 CUDA tensor (or N column tensors [n, 4])."""
+    cols = list(four) if not isinstance(four, torch.Tensor) else [four[k] for k in range(four.shape[0])]
+    if len(cols) != ch.n_daughters:
+        raise ValueError("need one column per daughter")
+    n = cols[0].shape[0]
+    for c in cols:
+        if c.dtype != torch.float64 or tuple(c.shape) != (n, 4) or not c.is_contiguous():
+            raise ValueError("columns must be contiguous float64 [n, 4]")
+    if weights is not None and (weights.dtype != torch.float64 or weights.numel() < n):
+        raise ValueError("weights must be float64 [n]")
+    if flags is not None and (flags.dtype != torch.uint8 or flags.numel() < n):
+        raise ValueError("flags must be uint8 [n]")
+    arr = _ptr_array(cols)
+    check(lib().hps_generate(ctypes.byref(ch), first, n, ctypes.cast(arr, ctypes.c_void_p), _dptr(weights),
+                             _dptr(flags), unweight_seed & (2**64 - 1), _PRECISIONS[precision],
+                             _stream_handle(stream)))
+
+
+def generate_host(ch: HpsChannel, first: int, four: torch.Tensor, weights=None, flags=None,
+                  unweight_seed: int = DEFAULT_UNWEIGHT_SEED, precision="fp64", chunk_events: int = 0,
+                  stream=None) -> None:
+    """Generate into HOST tensors (pinned for full link bandwidth): four [N, n, 4] float64 on CPU."""
+    if four.is_cuda or four.dtype != torch.float64 or four.dim() != 3 or four.shape[2] != 4:
+        raise ValueError("four must be a CPU float64 [N, n, 4] tensor")
+    if not four.is_contiguous():
+        raise ValueError("four must be contiguous")
+    N, n = four.shape[0], four.shape[1]
+    if N != ch.n_daughters:
+        raise ValueError("need one column per daughter")
+    arr = (ctypes.c_void_p * N)(*[four[k].data_ptr() for k in range(N)])
+    wp = ctypes.c_void_p(weights.data_ptr()) if weights is not None else ctypes.c_void_p(0)
+    fp = ctypes.c_void_p(flags.data_ptr()) if flags is not None else ctypes.c_void_p(0)
+    check(lib().hps_generate_host(ctypes.byref(ch), first, n, ctypes.cast(arr, ctypes.c_void_p), wp, fp,
+                                  unweight_seed & (2**64 - 1), _PRECISIONS[precision], chunk_events,
+                                  _stream_handle(stream)))
+
+
+def evaluate(ch: HpsChannel, first: int, n: int, functors: Sequence[HpsFunctor], weights: torch.Tensor | None,
+             outs: Sequence[torch.Tensor], precision="fp64", stream=None) -> None:
+    fa = (HpsFunctor * max(1, len(functors)))(*functors)
+    arr = _ptr_array(outs)
+    check(lib().hps_evaluate(ctypes.byref(ch), first, n, ctypes.cast(fa, ctypes.c_void_p), len(functors),
+                             _dptr(weights), ctypes.cast(arr, ctypes.c_void_p), _PRECISIONS[precision],
+                             _stream_handle(stream)))
+
+
+def average_on_workspace_size(n: int) -> int:
+    return int(lib().hps_average_on_workspace_size(n))
+
+
+def average_on(ch: HpsChannel, first: int, n: int, functor: HpsFunctor, out: torch.Tensor,
+               workspace: torch.Tensor | None = None, precision="fp64", stream=None) -> None:
+    """out: float64 CUDA tensor with >= 3 elements receiving {mean, M2, W}."""
+    if out.dtype != torch.float64 or out.numel() < 3:
+        raise ValueError("out must be float64 with 3 elements")
+    wbytes = 0 if workspace is None else workspace.numel() * workspace.element_size()
+    check(lib().hps_average_on(ctypes.byref(ch), first, n, ctypes.byref(functor), _dptr(out), _dptr(workspace),
+                               wbytes, _PRECISIONS[precision], _stream_handle(stream)))
+
+
+def event_weights(n_daughters: int, masses: Sequence[float], max_weight: float, four: torch.Tensor,
+                  out: torch.Tensor, stream=None) -> None:
+    n = four.shape[1]
+    arr = _ptr_array([four[k] for k in range(n_daughters)])
+    m = _double_array(masses)
+    check(lib().hps_event_weights(n_daughters, ctypes.cast(m, ctypes.c_void_p), max_weight, n,
+                                  ctypes.cast(arr, ctypes.c_void_p), _dptr(out), _stream_handle(stream)))
+
+
+def unweight_flags(n_daughters: int, masses: Sequence[float], max_weight: float, four: torch.Tensor,
+                   flags: torch.Tensor, unweight_seed: int = DEFAULT_UNWEIGHT_SEED, first: int = 0,
+                   stream=None) -> None:
+    n = four.shape[1]
+    arr = _ptr_array([four[k] for k in range(n_daughters)])
+    m = _double_array(masses)
+    check(lib().hps_unweight_flags(n_daughters, ctypes.cast(m, ctypes.c_void_p), max_weight, n,
+                                   ctypes.cast(arr, ctypes.c_void_p), unweight_seed & (2**64 - 1), first,
+                                   _dptr(flags), _stream_handle(stream)))
+
+
+def rng_words(n_daughters: int, engine, seed: int, first: int, n: int, out: torch.Tensor, stream=None) -> None:
+    if out.dtype not in (torch.int64, torch.uint64) or out.numel() < n * (3 * n_daughters - 4):
+        raise ValueError("out must be 64-bit with n*(3N-4) elements")
+    check(lib().hps_rng_words(n_daughters, _ENGINES[engine], int(seed) & (2**64 - 1), first, n, _dptr(out),
+                              _stream_handle(stream)))
+
+
+# ----------------------------------------------------------------------------- reference-shaped API
+
+@dataclass
+class Vector4R:
+    """(E, px, py, pz), hydra/Vector4R.h:59."""
+    e: float
+    px: float = 0.0
+    py: float = 0.0
+    pz: float = 0.0
+
+    def as_list(self):
+        return [self.e, self.px, self.py, self.pz]
+
+    def mass(self) -> float:
+        m2 = self.e * self.e - self.px * self.px - self.py * self.py - self.pz * self.pz
+        return math.sqrt(m2) if m2 > 0 else 0.0
+
+
+def _pdk(a, b, c):
+    x = (a - b - c) * (a + b + c) * (a - b + c) * (a + b - c)
+    return math.sqrt(x) / (2 * a)
+
+
+class Decays:
+    """N columns of Vector4R in device memory (hydra/Decays.h:67-651), plus the optional
+    generation-time weight column this implementation can store beside them."""
+
+    def __init__(self, mother_mass: float, masses: Sequence[float], nentries: int = 0, device="cuda",
+                 with_weights: bool = True):
+        self.mother_mass = float(mother_mass)
+        self.masses = [float(m) for m in masses]
+        ecm = self.mother_mass - sum(self.masses)
+        emmax, emmin, wtmax = ecm + self.masses[0], 0.0, 1.0
+        for i in range(1, len(self.masses)):          # Decays.h:100-118
+            emmin += self.masses[i - 1]
+            emmax += self.masses[i]
+            wtmax *= _pdk(emmax, emmin, self.masses[i])
+        self.max_weight = 1.0 / wtmax
+        self.four = torch.empty((len(self.masses), nentries, 4), dtype=torch.float64, device=device)
+        self.weights = torch.empty(nentries, dtype=torch.float64, device=device) if with_weights else None
+
+    def __len__(self):
+        return self.four.shape[1]
+
+    def size(self):
+        return len(self)
+
+    def GetMaxWeight(self):
+        return self.max_weight
+
+    def GetMotherMass(self):
+        return self.mother_mass
+
+    def GetMasses(self):
+        return list(self.masses)
+
+    def GetDaughters(self, k: int) -> torch.Tensor:
+        return self.four[k]
+
+    def __getitem__(self, i):
+        return tuple(Vector4R(*self.four[k, i].tolist()) for k in range(self.four.shape[0]))
+
+    def GetEventWeights(self, stream=None) -> torch.Tensor:
+        """Events | Events.GetEventWeightFunctor() (Decays.h:235-239), evaluated eagerly."""
+        out = torch.empty(len(self), dtype=torch.float64, device=self.four.device)
+        event_weights(len(self.masses), self.masses, self.max_weight, self.four, out, stream)
+        return out
+
+    def UnweightFlags(self, seed: int = DEFAULT_UNWEIGHT_SEED, stream=None) -> torch.Tensor:
+        flags = torch.empty(len(self), dtype=torch.uint8, device=self.four.device)
+        unweight_flags(len(self.masses), self.masses, self.max_weight, self.four, flags, seed, 0, stream)
+        return flags
+
+    def Unweight(self, seed: int = DEFAULT_UNWEIGHT_SEED) -> int:
+        """Decays::Unweight (Decays.inl:415-455): stable-partitions the accepted events to the
+        front and returns their count."""
+        flags = self.UnweightFlags(seed).bool()
+        order = torch.cat([torch.nonzero(flags).flatten(), torch.nonzero(~flags).flatten()])
+        self.four = self.four.index_select(1, order).contiguous()
+        if self.weights is not None:
+            self.weights = self.weights.index_select(0, order).contiguous()
+        return int(flags.sum().item())
+
+
+class PhaseSpace:
+    """hydra::PhaseSpace<N, GRND> (hydra/PhaseSpace.h:86-346)."""
+
+    def __init__(self, mother_mass: float, masses: Sequence[float], engine="default", precision="fp64"):
+        self.masses = [float(m) for m in masses]
+        self.N = len(self.masses)
+        self.engine = _ENGINES[engine]
+        self.precision = precision
+        self.mother_mass = float(mother_mass)
+        # validates and computes ECM / max weight exactly as the C++ constructor
+        ch = make_channel(self.masses, mother_mass, 0, self.engine)
+        self._ecm = ch.ecm
+        self._max_weight = ch.max_weight
+        self._seed = default_seed(self.masses)      # PhaseSpace.inl:44,64
+
+    # seeds are GInt_t through this API (PhaseSpace.h:285-291)
+    def SetSeed(self, seed: int) -> None:
+        s = int(seed) & 0xFFFFFFFF
+        s = s - (1 << 32) if s >= (1 << 31) else s
+        self._seed = s & (2**64 - 1)
+
+    def GetSeed(self) -> int:
+        s = self._seed & 0xFFFFFFFF
+        return s - (1 << 32) if s >= (1 << 31) else s
+
+    def GetMaxWeight(self):
+        return self._max_weight
+
+    def GetECM(self):
+        return self._ecm
+
+    def GetMasses(self):
+        return list(self.masses)
+
+    def GetMotherMass(self):
+        return self.mother_mass
+
+    def _channel(self, mother: Vector4R | Sequence[float] | None) -> HpsChannel:
+        mom = mother.as_list() if isinstance(mother, Vector4R) else (
+            list(mother) if mother is not None else [self.mother_mass, 0.0, 0.0, 0.0])
+        ch = make_channel(self.masses, self.mother_mass, self._seed, self.engine, mom)
+        ch.max_weight = self._max_weight
+        ch.ecm = self._ecm
+        return ch
+
+    def Generate(self, mother, events: Decays | int, flags: torch.Tensor | None = None,
+                 unweight_seed: int = DEFAULT_UNWEIGHT_SEED) -> Decays:
+        if isinstance(events, int):
+            events = Decays(self.mother_mass, self.masses, events)
+        generate(self._channel(mother), 0, events.four, events.weights, flags, unweight_seed, self.precision)
+        torch.cuda.current_stream().synchronize()
+        return events
+
+    def AverageOn(self, mother, functor: HpsFunctor, n: int):
+        out = torch.zeros(3, dtype=torch.float64, device="cuda")
+        average_on(self._channel(mother), 0, n, functor, out, None, self.precision)
+        mean, m2, w = out.tolist()
+        return mean, (math.sqrt(m2) / w if w != 0 else float("nan"))
+
+    def Evaluate(self, mother, n: int, *functors: HpsFunctor) -> torch.Tensor:
+        res = torch.empty((len(functors) + 1, n), dtype=torch.float64, device="cuda")
+        evaluate(self._channel(mother), 0, n, functors, res[0], [res[k + 1] for k in range(len(functors))],
+                 self.precision)
+        torch.cuda.current_stream().synchronize()
+        return res

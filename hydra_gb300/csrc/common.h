@@ -1,0 +1,65 @@
+// common.h -- host-side helpers shared by the C-ABI translation units of libhps.so.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "../../include/hps.h"
+#include "genbod.cuh"
+
+namespace hps {
+
+// Per-thread message behind hps_last_error().
+hps_status set_error(hps_status st, const char* fmt, ...);
+void clear_error();
+
+inline hps_status cuda_status(cudaError_t e, const char* what)
+{
+    if (e == cudaSuccess) return HPS_OK;
+    return set_error(HPS_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+// Validates the channel and converts it to the kernel-side form.
+hps_status to_device_channel(const hps_channel* ch, DevChannel* out);
+hps_status to_device_functor(const hps_functor* f, int n_daughters, DevFunctor* out);
+
+inline bool range_ok(uint64_t first, uint64_t n) { return first + n >= first; }
+
+inline bool aligned(const void* p, size_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// Grid for a one-thread-per-item kernel with a grid-stride loop: enough CTAs to fill
+// the device several times over, never more than the work needs.
+inline unsigned grid_for(uint64_t items, unsigned threads, unsigned max_ctas = 152u * 32u)
+{
+    const uint64_t need = (items + threads - 1) / threads;
+    return static_cast<unsigned>(need < max_ctas ? (need == 0 ? 1 : need) : max_ctas);
+}
+
+// Instantiates BODY(N, ENGINE) for the runtime (n_daughters, engine) pair.
+#define HPS_DISPATCH_N_ENGINE(n_daughters, engine, BODY)                         \
+    switch ((n_daughters) * 2 + ((engine) == 0 ? 0 : 1)) {                      \
+    case 4:  BODY(2, 0)  break; case 5:  BODY(2, 1)  break;                     \
+    case 6:  BODY(3, 0)  break; case 7:  BODY(3, 1)  break;                     \
+    case 8:  BODY(4, 0)  break; case 9:  BODY(4, 1)  break;                     \
+    case 10: BODY(5, 0)  break; case 11: BODY(5, 1)  break;                     \
+    case 12: BODY(6, 0)  break; case 13: BODY(6, 1)  break;                     \
+    case 14: BODY(7, 0)  break; case 15: BODY(7, 1)  break;                     \
+    case 16: BODY(8, 0)  break; case 17: BODY(8, 1)  break;                     \
+    case 18: BODY(9, 0)  break; case 19: BODY(9, 1)  break;                     \
+    case 20: BODY(10, 0) break; case 21: BODY(10, 1) break;                     \
+    default: return set_error(HPS_ERR_BAD_ARG, "n_daughters %d outside 2..10", (int)(n_daughters)); \
+    }
+
+#define HPS_DISPATCH_N(n_daughters, BODY)                                        \
+    switch (n_daughters) {                                                      \
+    case 2: BODY(2) break; case 3: BODY(3) break; case 4: BODY(4) break;        \
+    case 5: BODY(5) break; case 6: BODY(6) break; case 7: BODY(7) break;        \
+    case 8: BODY(8) break; case 9: BODY(9) break; case 10: BODY(10) break;      \
+    default: return set_error(HPS_ERR_BAD_ARG, "n_daughters %d outside 2..10", (int)(n_daughters)); \
+    }
+
+}  // namespace hps

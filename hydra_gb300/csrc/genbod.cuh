@@ -1,0 +1,208 @@
+// genbod.cuh -- per-event Raubold-Lynch (GENBOD) body, FP64 form.
+//
+// Restates hydra::detail::DecayMother<N,GRND>::process (hydra/detail/functors/DecayMother.h:163-277;
+// AverageMother.h:156-270 and EvalMother.h:169-283 are the same body) for one event held in
+// registers.  The FP64 form issues every double operation that can round as a separately
+// rounded IEEE operation in the reference's order (__dadd_rn / __dmul_rn / __dsqrt_rn /
+// __ddiv_rn, no FMA contraction), so invariant masses, pdk momenta, the event weight,
+// energies, rotations and boosts round exactly as the reference built without FMA
+// contraction.  The only operations whose last bit may differ are cos/sin of the azimuth
+// (CUDA's sincos versus the host libm).
+#pragma once
+#include <cstdint>
+#include "rng.cuh"
+
+namespace hps {
+
+// Channel constants as the kernels see them (passed by value as a kernel parameter).
+struct DevChannel {
+    double masses[10];
+    double ecm;
+    double max_weight;
+    double beta[3];       // final-boost vector (DecayMother.h:88-98)
+    uint64_t key;         // splitmix64(seed): Philox key / squares3 key
+    int boost_active;     // 0 < |beta|^2 < 1: only then does applyBoostTo change anything
+};
+
+namespace f64 {
+
+__device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double dvd(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ double sqr(double a) { return __dsqrt_rn(a); }
+
+// DecayMother::pdk (DecayMother.h:119-126): sqrt((a-b-c)(a+b+c)(a-b+c)(a+b-c)) / (2a).
+__device__ __forceinline__ double pdk(double a, double b, double c)
+{
+    const double amb = sub(a, b), apb = add(a, b);
+    const double x = mul(mul(mul(sub(amb, c), add(apb, c)), add(amb, c)), sub(apb, c));
+    return dvd(sqr(x), mul(2.0, a));
+}
+
+// Vector4R::applyBoostTo(Vector3R(bx,by,bz)) (hydra/detail/Vector4R.inl:249-310), general form.
+__device__ __forceinline__ void boost_general(double (&v)[4], double bx, double by, double bz)
+{
+    const double bxx = mul(bx, bx), byy = mul(by, by), bzz = mul(bz, bz);
+    const double b2 = add(add(bxx, byy), bzz);
+    if (b2 > 0.0 && b2 < 1.0) {
+        const double gamma = dvd(1.0, sqr(sub(1.0, b2)));
+        const double gb2 = dvd(sub(gamma, 1.0), b2);
+        const double gb2xy = mul(mul(gb2, bx), by);
+        const double gb2xz = mul(mul(gb2, bx), bz);
+        const double gb2yz = mul(mul(gb2, by), bz);
+        const double gbx = mul(gamma, bx), gby = mul(gamma, by), gbz = mul(gamma, bz);
+        const double e2 = v[0], px2 = v[1], py2 = v[2], pz2 = v[3];
+        v[0] = add(add(add(mul(gamma, e2), mul(gbx, px2)), mul(gby, py2)), mul(gbz, pz2));
+        v[1] = add(add(add(add(mul(gbx, e2), mul(mul(gb2, bxx), px2)), px2), mul(gb2xy, py2)),
+                   mul(gb2xz, pz2));
+        v[2] = add(add(add(add(mul(gby, e2), mul(mul(gb2, byy), py2)), py2), mul(gb2xy, px2)),
+                   mul(gb2yz, pz2));
+        v[3] = add(add(add(add(mul(gbz, e2), mul(mul(gb2, bzz), pz2)), pz2), mul(gb2yz, py2)),
+                   mul(gb2xz, px2));
+    }
+}
+
+// Vector4R::mass (Vector4R.inl:195-209).
+__device__ __forceinline__ double mass(const double (&v)[4])
+{
+    const double m2 = sub(sub(sub(mul(v[0], v[0]), mul(v[1], v[1])), mul(v[2], v[2])), mul(v[3], v[3]));
+    return (m2 > 0.0) ? sqr(m2) : 0.0;
+}
+
+__device__ __forceinline__ double mass2(const double (&v)[4])
+{
+    return sub(sub(sub(mul(v[0], v[0]), mul(v[1], v[1])), mul(v[2], v[2])), mul(v[3], v[3]));
+}
+
+// One event.  p[k] = {E, px, py, pz} of daughter k.  Returns the generation-time weight.
+template <int N, int ENGINE>
+__device__ __forceinline__ double event(const DevChannel& ch, uint64_t evt, double (&p)[N][4])
+{
+    constexpr int NW = 3 * N - 4;
+    uint64_t w[NW];
+    event_words<N, ENGINE>(ch.key, evt, w);
+    if constexpr (N > 3) sort_words<N - 2>(w);
+
+    // invariant masses of the intermediate systems (DecayMother.h:170-197)
+    double invMas[N];
+    {
+        double sum = 0.0;
+#pragma unroll
+        for (int n = 0; n < N; ++n) {
+            const double rno = (n == 0) ? 0.0 : (n == N - 1) ? 1.0 : word_to_uniform<ENGINE>(w[n - 1]);
+            sum = add(sum, ch.masses[n]);
+            invMas[n] = add(mul(rno, ch.ecm), sum);
+        }
+    }
+    // weight (DecayMother.h:203-212)
+    double pd[N - 1];
+    double wt = ch.max_weight;
+#pragma unroll
+    for (int n = 0; n < N - 1; ++n) {
+        pd[n] = pdk(invMas[n + 1], invMas[n], ch.masses[n + 1]);
+        wt = mul(wt, pd[n]);
+    }
+    // Raubold-Lynch construction (DecayMother.h:218-257)
+    p[0][0] = sqr(add(mul(pd[0], pd[0]), mul(ch.masses[0], ch.masses[0])));
+    p[0][1] = 0.0; p[0][2] = pd[0]; p[0][3] = 0.0;
+#pragma unroll
+    for (int i = 1; i < N; ++i) {
+        p[i][0] = sqr(add(mul(pd[i - 1], pd[i - 1]), mul(ch.masses[i], ch.masses[i])));
+        p[i][1] = 0.0; p[i][2] = -pd[i - 1]; p[i][3] = 0.0;
+
+        const double cZ = sub(mul(2.0, word_to_uniform<ENGINE>(w[N - 2 + 2 * (i - 1)])), 1.0);
+        const double sZ = sqr(sub(1.0, mul(cZ, cZ)));
+        const double angY = mul(2.0 * 3.1415926535897932384626422832795028841971,
+                                word_to_uniform<ENGINE>(w[N - 2 + 2 * (i - 1) + 1]));
+        double sY, cY;
+        sincos(angY, &sY, &cY);
+#pragma unroll
+        for (int j = 0; j <= i; ++j) {
+            const double x = p[j][1], y = p[j][2];
+            const double x1 = sub(mul(cZ, x), mul(sZ, y));
+            p[j][2] = add(mul(sZ, x), mul(cZ, y));
+            const double z = p[j][3];
+            p[j][1] = sub(mul(cY, x1), mul(sY, z));
+            p[j][3] = add(mul(sY, x1), mul(cY, z));
+        }
+        if (i == N - 1) break;
+        // boost along y by beta = pd/E of the (0..i) system: applyBoostTo(Vector3R(0, beta, 0))
+        // with the zero components folded (adding a signed zero to a non-zero sum is exact).
+        const double beta = dvd(pd[i], sqr(add(mul(pd[i], pd[i]), mul(invMas[i], invMas[i]))));
+        const double b2 = mul(beta, beta);
+        if (b2 > 0.0 && b2 < 1.0) {
+            const double gamma = dvd(1.0, sqr(sub(1.0, b2)));
+            const double gby = mul(gamma, beta);
+            const double gb2byy = mul(dvd(sub(gamma, 1.0), b2), b2);
+#pragma unroll
+            for (int j = 0; j <= i; ++j) {
+                const double e2 = p[j][0], py2 = p[j][2];
+                p[j][0] = add(mul(gamma, e2), mul(gby, py2));
+                p[j][2] = add(add(mul(gby, e2), mul(gb2byy, py2)), py2);
+            }
+        }
+    }
+    // final boost to the mother's frame (DecayMother.h:264-269)
+    if (ch.boost_active) {
+#pragma unroll
+        for (int n = 0; n < N; ++n) boost_general(p[n], ch.beta[0], ch.beta[1], ch.beta[2]);
+    }
+    return wt;
+}
+
+// PhaseSpaceWeight::Evaluate (hydra/detail/Decays.inl:215-231): weight recomputed from
+// stored four-vectors, R the running sum of daughters.
+template <int N>
+__device__ __forceinline__ double recomputed_weight(const double* masses, double max_weight,
+                                                    const double (&p)[N][4])
+{
+    double R[4] = {p[0][0], p[0][1], p[0][2], p[0][3]};
+    double w = max_weight;
+#pragma unroll
+    for (int i = 1; i < N; ++i) {
+        double S[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) S[c] = add(R[c], p[i][c]);
+        w = mul(w, pdk(mass(S), masses[i], mass(R)));
+#pragma unroll
+        for (int c = 0; c < 4; ++c) R[c] = S[c];
+    }
+    return w;
+}
+
+}  // namespace f64
+
+// Functor menu (include/hps.h, hps_functor): 1, mass2(p_i+p_j), |BW(mass2(p_i+p_j))|^2.
+struct DevFunctor {
+    int kind, i, j;
+    double a, b;
+};
+
+template <int N>
+__device__ __forceinline__ double functor_f64(const DevFunctor& f, const double (&p)[N][4])
+{
+    if (f.kind == 0) return 1.0;
+    double s[4];
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        if (k == f.i) {
+#pragma unroll
+            for (int c = 0; c < 4; ++c) s[c] = p[k][c];
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        if (k == f.j) {
+#pragma unroll
+            for (int c = 0; c < 4; ++c) s[c] = f64::add(s[c], p[k][c]);
+        }
+    }
+    const double m2 = f64::mass2(s);
+    if (f.kind == 1) return m2;
+    const double d = f64::sub(f64::mul(f.a, f.a), m2);
+    const double g = f64::mul(f.a, f.b);
+    return f64::dvd(1.0, f64::add(f64::mul(d, d), f64::mul(g, g)));
+}
+
+}  // namespace hps

@@ -1,0 +1,130 @@
+// hps_average.cu -- storage-free AverageOn.
+//
+// Replaces hydra::detail::launch_reducer -> thrust::transform_reduce(counting, AverageMother,
+// StatsPHSP(), AddStatsPHSP()) (hydra/detail/launch_decayers.inl:94-106, PhaseSpace.inl:255-273).
+// Each event is generated and weighted in registers, mapped to StatsPHSP{f, w, 0}
+// (AverageMother.h:272-292) and merged with AddStatsPHSP.  The merge tree is fixed by the
+// event count alone:
+//   tile t = events [t*4096, (t+1)*4096); thread j of the 256-thread CTA folds events
+//   t*4096 + j + 256*k, k = 0..15, in order; a fixed warp/CTA tree merges the 256 folds;
+//   the tile partials are merged by one CTA in a fixed tree.
+// Which CTA runs which tile does not matter, so the result is bit-identical for every grid.
+#include "common.h"
+#include "store.cuh"
+
+namespace hps {
+
+constexpr int kAvgThreads = 256;
+constexpr int kAvgPerThread = HPS_AVG_TILE / kAvgThreads;
+static_assert(kAvgThreads * kAvgPerThread == HPS_AVG_TILE, "tile shape");
+constexpr int kFinalThreads = 1024;
+
+template <int N, int ENGINE>
+__global__ void __launch_bounds__(kAvgThreads)
+k_average_tiles_f64(DevChannel ch, DevFunctor fn, uint64_t first, uint64_t n, uint64_t ntiles,
+                    hps_stats* __restrict__ partials)
+{
+    for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        hps_stats acc{0.0, 0.0, 0.0};
+        const uint64_t base = t * HPS_AVG_TILE + threadIdx.x;
+        for (int k = 0; k < kAvgPerThread; ++k) {
+            const uint64_t e = base + (uint64_t)k * kAvgThreads;
+            if (e < n) {
+                double p[N][4];
+                hps_stats y;
+                y.w = f64::event<N, ENGINE>(ch, first + e, p);
+                y.mean = functor_f64<N>(fn, p);
+                y.m2 = 0.0;
+                acc = stats_merge(acc, y);
+            }
+        }
+        const hps_stats r = block_reduce_stats<kAvgThreads>(acc);
+        if (threadIdx.x == 0) partials[t] = r;
+    }
+}
+
+// One CTA: thread j folds partials j, j+1024, ... in order, then the fixed CTA tree.
+__global__ void __launch_bounds__(kFinalThreads)
+k_average_final(const hps_stats* __restrict__ partials, uint64_t ntiles, hps_stats* __restrict__ out)
+{
+    hps_stats acc{0.0, 0.0, 0.0};
+    for (uint64_t t = threadIdx.x; t < ntiles; t += kFinalThreads) acc = stats_merge(acc, partials[t]);
+    const hps_stats r = block_reduce_stats<kFinalThreads>(acc);
+    if (threadIdx.x == 0) *out = r;
+}
+
+// Host-side validation shared by every AverageOn entry point; touches no device state.
+hps_status average_args(const hps_channel* channel, const hps_functor* functor, int32_t precision,
+                        DevChannel* ch, DevFunctor* fn)
+{
+    hps_status st = to_device_channel(channel, ch);
+    if (st != HPS_OK) return st;
+    st = to_device_functor(functor, channel->n_daughters, fn);
+    if (st != HPS_OK) return st;
+    if (precision != HPS_PREC_FP64 && precision != HPS_PREC_FP32_FIX)
+        return set_error(HPS_ERR_BAD_ARG, "unknown precision %d", precision);
+    if (precision == HPS_PREC_FP32_FIX)
+        return set_error(HPS_ERR_UNSUPPORTED, "FP32_FIX average not built yet");
+    return HPS_OK;
+}
+
+hps_status launch_average(const hps_channel* channel, const DevChannel& ch, const DevFunctor& fn,
+                          uint64_t first_evt, uint64_t n, hps_stats* out, hps_stats* partials,
+                          cudaStream_t stream)
+{
+    const uint64_t ntiles = (n + HPS_AVG_TILE - 1) / HPS_AVG_TILE;
+    if (ntiles > 0) {
+        const unsigned grid = static_cast<unsigned>(ntiles < 152u * 16u ? ntiles : 152u * 16u);
+#define HPS_BODY(NN, EE)                                                                           \
+    k_average_tiles_f64<NN, EE><<<grid, kAvgThreads, 0, stream>>>(ch, fn, first_evt, n, ntiles, partials);
+        HPS_DISPATCH_N_ENGINE(channel->n_daughters, channel->engine, HPS_BODY)
+#undef HPS_BODY
+    }
+    k_average_final<<<1, kFinalThreads, 0, stream>>>(partials, ntiles, out);
+    return cuda_status(cudaGetLastError(), "hps_average_on launch");
+}
+
+}  // namespace hps
+
+using namespace hps;
+
+extern "C" {
+
+size_t hps_average_on_workspace_size(uint64_t n)
+{
+    const uint64_t ntiles = (n + HPS_AVG_TILE - 1) / HPS_AVG_TILE;
+    return static_cast<size_t>((ntiles == 0 ? 1 : ntiles) * sizeof(hps_stats));
+}
+
+hps_status hps_average_on(const hps_channel* channel, uint64_t first_evt, uint64_t n, const hps_functor* functor,
+                          hps_stats* out, void* workspace, size_t workspace_bytes, int32_t precision, void* stream)
+{
+    clear_error();
+    DevChannel ch;
+    DevFunctor fn;
+    hps_status st = average_args(channel, functor, precision, &ch, &fn);
+    if (st != HPS_OK) return st;
+    if (!out) return set_error(HPS_ERR_BAD_ARG, "out is NULL");
+    if (!range_ok(first_evt, n)) return set_error(HPS_ERR_BAD_ARG, "event range wraps 2^64");
+    if (!aligned(out, 8)) return set_error(HPS_ERR_BAD_ARG, "out not 8-byte aligned");
+    const size_t need = hps_average_on_workspace_size(n);
+    cudaStream_t s = as_stream(stream);
+    if (workspace) {
+        if (workspace_bytes < need)
+            return set_error(HPS_ERR_BAD_ARG, "workspace of %zu bytes, %zu needed", workspace_bytes, need);
+        if (!aligned(workspace, 8)) return set_error(HPS_ERR_BAD_ARG, "workspace not 8-byte aligned");
+        return launch_average(channel, ch, fn, first_evt, n, out, static_cast<hps_stats*>(workspace), s);
+    }
+    void* scratch = nullptr;
+    cudaError_t e = cudaMallocAsync(&scratch, need, s);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(HPS_ERR_OOM, "cudaMallocAsync(%zu): %s", need, cudaGetErrorString(e));
+    }
+    st = launch_average(channel, ch, fn, first_evt, n, out, static_cast<hps_stats*>(scratch), s);
+    e = cudaFreeAsync(scratch, s);
+    if (st == HPS_OK && e != cudaSuccess) return cuda_status(e, "cudaFreeAsync");
+    return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,243 @@
+// hps_generate.cu -- Generate (store path) and Evaluate entry points.
+//
+// Generate replaces hydra::detail::launch_decayer -> thrust::tabulate(Decays, DecayMother)
+// (hydra/detail/launch_decayers.inl:133-149); Evaluate replaces launch_evaluator ->
+// thrust::tabulate(multivector, EvalMother) (launch_decayers.inl:66-72).  One thread owns
+// one event; events of a warp are consecutive, so every column store of a warp is one
+// contiguous 1 KiB span.
+#include <mutex>
+
+#include "common.h"
+#include "store.cuh"
+
+namespace hps {
+
+struct Cols { double* p[HPS_MAX_DAUGHTERS]; };
+
+template <int N, int ENGINE>
+__global__ void __launch_bounds__(256)
+k_generate_f64(DevChannel ch, Cols cols, double* __restrict__ weights, uint8_t* __restrict__ flags,
+               uint64_t ukey, uint64_t first, uint64_t n, int vec32)
+{
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < n;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        double p[N][4];
+        const double wt = f64::event<N, ENGINE>(ch, first + e, p);
+#pragma unroll
+        for (int k = 0; k < N; ++k) store_vec4(cols.p[k], e, p[k], vec32 != 0);
+        if (weights) weights[e] = wt;
+        if (flags) {
+            // FlagDaugthers (hydra/detail/Decays.inl:77-89) on the event just stored.
+            const double wr = f64::recomputed_weight<N>(ch.masses, ch.max_weight, p);
+            const double u = static_cast<double>(squares3_word(ukey, first + e)) * 0x1p-32;
+            flags[e] = (f64::dvd(wr, ch.max_weight) > u) ? 1 : 0;
+        }
+    }
+}
+
+constexpr int kMaxFunctors = 8;
+struct Functors { DevFunctor f[kMaxFunctors]; };
+struct OutCols { double* p[kMaxFunctors]; };
+
+template <int N, int ENGINE>
+__global__ void __launch_bounds__(256)
+k_evaluate_f64(DevChannel ch, Functors fs, int nf, double* __restrict__ weights, OutCols out,
+               uint64_t first, uint64_t n)
+{
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < n;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        double p[N][4];
+        const double wt = f64::event<N, ENGINE>(ch, first + e, p);
+        if (weights) weights[e] = wt;
+        for (int k = 0; k < nf; ++k) out.p[k][e] = functor_f64<N>(fs.f[k], p);
+    }
+}
+
+}  // namespace hps
+
+using namespace hps;
+
+extern "C" {
+
+hps_status hps_generate(const hps_channel* channel, uint64_t first_evt, uint64_t n, double* const* cols,
+                        double* weights, uint8_t* flags, uint64_t unweight_seed, int32_t precision,
+                        void* stream)
+{
+    clear_error();
+    DevChannel ch;
+    hps_status st = to_device_channel(channel, &ch);
+    if (st != HPS_OK) return st;
+    if (precision != HPS_PREC_FP64 && precision != HPS_PREC_FP32_FIX)
+        return set_error(HPS_ERR_BAD_ARG, "unknown precision %d", precision);
+    if (!range_ok(first_evt, n)) return set_error(HPS_ERR_BAD_ARG, "event range wraps 2^64");
+    if (n == 0) return HPS_OK;
+    if (!cols) return set_error(HPS_ERR_BAD_ARG, "cols is NULL");
+    const int N = channel->n_daughters;
+    Cols cc{};
+    bool all32 = true;
+    for (int k = 0; k < N; ++k) {
+        if (!cols[k]) return set_error(HPS_ERR_BAD_ARG, "column %d is NULL", k);
+        if (!aligned(cols[k], 16)) return set_error(HPS_ERR_BAD_ARG, "column %d not 16-byte aligned", k);
+        all32 = all32 && aligned(cols[k], 32);
+        cc.p[k] = cols[k];
+    }
+    if (weights && !aligned(weights, 8)) return set_error(HPS_ERR_BAD_ARG, "weights not 8-byte aligned");
+    if (precision == HPS_PREC_FP32_FIX)
+        return set_error(HPS_ERR_UNSUPPORTED, "FP32_FIX generate not built yet");
+    const uint64_t ukey = splitmix64(unweight_seed);
+    const unsigned grid = grid_for(n, 256);
+    const int vec32 = all32 ? 1 : 0;
+#define HPS_BODY(NN, EE)                                                                  \
+    k_generate_f64<NN, EE><<<grid, 256, 0, as_stream(stream)>>>(ch, cc, weights, flags, ukey, \
+                                                                 first_evt, n, vec32);
+    HPS_DISPATCH_N_ENGINE(N, channel->engine, HPS_BODY)
+#undef HPS_BODY
+    return cuda_status(cudaGetLastError(), "hps_generate launch");
+}
+
+hps_status hps_evaluate(const hps_channel* channel, uint64_t first_evt, uint64_t n, const hps_functor* functors,
+                        int32_t n_functors, double* weights, double* const* out, int32_t precision, void* stream)
+{
+    clear_error();
+    DevChannel ch;
+    hps_status st = to_device_channel(channel, &ch);
+    if (st != HPS_OK) return st;
+    if (precision != HPS_PREC_FP64 && precision != HPS_PREC_FP32_FIX)
+        return set_error(HPS_ERR_BAD_ARG, "unknown precision %d", precision);
+    if (n_functors < 0 || n_functors > kMaxFunctors)
+        return set_error(HPS_ERR_BAD_ARG, "n_functors %d outside 0..%d", n_functors, kMaxFunctors);
+    if (!range_ok(first_evt, n)) return set_error(HPS_ERR_BAD_ARG, "event range wraps 2^64");
+    if (n == 0) return HPS_OK;
+    const int N = channel->n_daughters;
+    Functors fs{};
+    OutCols oc{};
+    for (int k = 0; k < n_functors; ++k) {
+        st = to_device_functor(functors + k, N, &fs.f[k]);
+        if (st != HPS_OK) return st;
+        if (!out || !out[k]) return set_error(HPS_ERR_BAD_ARG, "output column %d is NULL", k);
+        oc.p[k] = out[k];
+    }
+    if (precision == HPS_PREC_FP32_FIX)
+        return set_error(HPS_ERR_UNSUPPORTED, "FP32_FIX evaluate not built yet");
+    const unsigned grid = grid_for(n, 256);
+#define HPS_BODY(NN, EE)                                                                          \
+    k_evaluate_f64<NN, EE><<<grid, 256, 0, as_stream(stream)>>>(ch, fs, n_functors, weights, oc, \
+                                                                 first_evt, n);
+    HPS_DISPATCH_N_ENGINE(N, channel->engine, HPS_BODY)
+#undef HPS_BODY
+    return cuda_status(cudaGetLastError(), "hps_evaluate launch");
+}
+
+}  // extern "C"
+
+namespace hps {
+
+// Per-device copy stream of the host-output pipeline, created on first use.  Events are
+// per call, so concurrent calls from several host threads do not share state.
+struct HostPipe {
+    cudaStream_t copy = nullptr;
+    cudaEvent_t gen_done[2] = {nullptr, nullptr};
+    cudaEvent_t copy_done[2] = {nullptr, nullptr};
+    ~HostPipe()
+    {
+        for (int b = 0; b < 2; ++b) {
+            if (gen_done[b]) cudaEventDestroy(gen_done[b]);
+            if (copy_done[b]) cudaEventDestroy(copy_done[b]);
+        }
+    }
+};
+
+static hps_status copy_stream(cudaStream_t* out)
+{
+    static std::mutex mu;
+    static cudaStream_t streams[64];
+    static bool ready[64] = {false};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_status(e, "cudaGetDevice");
+    if (dev < 0 || dev >= 64) return set_error(HPS_ERR_UNSUPPORTED, "device ordinal %d", dev);
+    std::lock_guard<std::mutex> lock(mu);
+    if (!ready[dev]) {
+        if ((e = cudaStreamCreateWithFlags(&streams[dev], cudaStreamNonBlocking)) != cudaSuccess)
+            return cuda_status(e, "cudaStreamCreate");
+        ready[dev] = true;
+    }
+    *out = streams[dev];
+    return HPS_OK;
+}
+
+}  // namespace hps
+
+extern "C" hps_status hps_generate_host(const hps_channel* channel, uint64_t first_evt, uint64_t n,
+                                        double* const* host_cols, double* host_weights, uint8_t* host_flags,
+                                        uint64_t unweight_seed, int32_t precision, uint64_t chunk_events,
+                                        void* stream)
+{
+    clear_error();
+    DevChannel ch;
+    hps_status st = to_device_channel(channel, &ch);
+    if (st != HPS_OK) return st;
+    if (!range_ok(first_evt, n)) return set_error(HPS_ERR_BAD_ARG, "event range wraps 2^64");
+    if (n == 0) return HPS_OK;
+    const int N = channel->n_daughters;
+    if (!host_cols) return set_error(HPS_ERR_BAD_ARG, "host_cols is NULL");
+    for (int k = 0; k < N; ++k)
+        if (!host_cols[k]) return set_error(HPS_ERR_BAD_ARG, "host column %d is NULL", k);
+    const uint64_t chunk = chunk_events ? chunk_events : (uint64_t(1) << 20);
+    // staging: N columns of 32 B/event (32-byte aligned), then weights, then flags
+    const size_t col_bytes = (size_t)chunk * 32;
+    const size_t buf_bytes = col_bytes * N + (size_t)chunk * 8 + ((size_t)chunk + 255) / 256 * 256;
+    HostPipe pipeobj;
+    HostPipe* pipe = &pipeobj;
+    if ((st = copy_stream(&pipe->copy)) != HPS_OK) return st;
+    for (int b = 0; b < 2; ++b) {
+        cudaError_t ee;
+        if ((ee = cudaEventCreateWithFlags(&pipe->gen_done[b], cudaEventDisableTiming)) != cudaSuccess ||
+            (ee = cudaEventCreateWithFlags(&pipe->copy_done[b], cudaEventDisableTiming)) != cudaSuccess)
+            return cuda_status(ee, "cudaEventCreate");
+    }
+    cudaStream_t s = as_stream(stream);
+    void* staging = nullptr;
+    cudaError_t e = cudaMallocAsync(&staging, 2 * buf_bytes, s);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(HPS_ERR_OOM, "staging cudaMallocAsync(%zu): %s", 2 * buf_bytes, cudaGetErrorString(e));
+    }
+    const uint64_t nchunks = (n + chunk - 1) / chunk;
+    for (uint64_t c = 0; c < nchunks && st == HPS_OK; ++c) {
+        const int b = static_cast<int>(c & 1);
+        const uint64_t off = c * chunk;
+        const uint64_t m = (n - off < chunk) ? (n - off) : chunk;
+        char* base = static_cast<char*>(staging) + b * buf_bytes;
+        double* dcols[HPS_MAX_DAUGHTERS];
+        for (int k = 0; k < N; ++k) dcols[k] = reinterpret_cast<double*>(base + k * col_bytes);
+        double* dw = host_weights ? reinterpret_cast<double*>(base + N * col_bytes) : nullptr;
+        uint8_t* df = host_flags ? reinterpret_cast<uint8_t*>(base + N * col_bytes + chunk * 8) : nullptr;
+        if (c >= 2 && (e = cudaStreamWaitEvent(s, pipe->copy_done[b], 0)) != cudaSuccess) {
+            st = cuda_status(e, "cudaStreamWaitEvent");
+            break;
+        }
+        st = hps_generate(channel, first_evt + off, m, dcols, dw, df, unweight_seed, precision, stream);
+        if (st != HPS_OK) break;
+        if ((e = cudaEventRecord(pipe->gen_done[b], s)) != cudaSuccess ||
+            (e = cudaStreamWaitEvent(pipe->copy, pipe->gen_done[b], 0)) != cudaSuccess) {
+            st = cuda_status(e, "pipeline event");
+            break;
+        }
+        for (int k = 0; k < N && e == cudaSuccess; ++k)
+            e = cudaMemcpyAsync(host_cols[k] + 4 * off, dcols[k], m * 32, cudaMemcpyDeviceToHost, pipe->copy);
+        if (e == cudaSuccess && dw)
+            e = cudaMemcpyAsync(host_weights + off, dw, m * 8, cudaMemcpyDeviceToHost, pipe->copy);
+        if (e == cudaSuccess && df)
+            e = cudaMemcpyAsync(host_flags + off, df, m, cudaMemcpyDeviceToHost, pipe->copy);
+        if (e == cudaSuccess) e = cudaEventRecord(pipe->copy_done[b], pipe->copy);
+        if (e != cudaSuccess) st = cuda_status(e, "device-to-host copy");
+    }
+    // the staging buffers may be released only after the last copies read them
+    for (int b = 0; b < 2 && b < (int)nchunks; ++b) cudaStreamWaitEvent(s, pipe->copy_done[b], 0);
+    e = cudaFreeAsync(staging, s);
+    if (st == HPS_OK && e != cudaSuccess) st = cuda_status(e, "cudaFreeAsync");
+    e = cudaStreamSynchronize(s);
+    if (st == HPS_OK && e != cudaSuccess) st = cuda_status(e, "cudaStreamSynchronize");
+    return st;
+}

@@ -1,0 +1,113 @@
+// rng.cuh -- counter-based random streams of the phase-space generator.
+//
+// Bit-exact with Hydra's engines as DecayMother uses them
+// (hydra/detail/functors/DecayMother.h:166-168: construct from the seed, discard(evt+3N)):
+//   * splitmix64 key derivation   hydra/detail/random/splitmix.h:56-61
+//   * Philox2x64, 7 rounds        hydra/detail/external/hydra_R123/philox.h:266-268,281-358
+//     EngineR123 pre-increments its 128-bit counter before each 2-word block
+//     (EngineR123.h:149-166, array.h:151-183), so event evt reads blocks at
+//     counters evt+3N+1, evt+3N+2, ... two 64-bit words each.
+//   * squares3                    hydra/detail/random/squares3.h:104-125: one 32-bit word
+//     per counter, counters evt+3N, evt+3N+1, ...
+//   * uniform on [0,1)            hydra_thrust/random/detail/uniform_real_distribution.inl:70-79:
+//     double(x) / 2^64 (Philox: double(2^64-1) rounds to 2^64) or x / 2^32 (squares3).
+#pragma once
+#include <cstdint>
+
+namespace hps {
+
+enum : int { kPhilox = 0, kSquares3 = 1 };
+
+__host__ __device__ __forceinline__ uint64_t splitmix64(uint64_t x)
+{
+    uint64_t z = x + 0x9e3779b97f4a7c15ULL;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    return z ^ (z >> 31);
+}
+
+// Philox2x64 bijection with 7 rounds: round = (hi(M*c0) ^ key ^ c1, lo(M*c0)),
+// key bumped by the golden-ratio Weyl constant between rounds.
+__device__ __forceinline__ void philox2x64_7(uint64_t c0, uint64_t c1, uint64_t key,
+                                             uint64_t& o0, uint64_t& o1)
+{
+    constexpr uint64_t M = 0xD2B74407B1CE6E93ULL;
+    constexpr uint64_t W = 0x9E3779B97F4A7C15ULL;
+#pragma unroll
+    for (int r = 0; r < 7; ++r) {
+        if (r > 0) key += W;
+        const uint64_t hi = __umul64hi(M, c0);
+        const uint64_t lo = M * c0;
+        c0 = hi ^ key ^ c1;
+        c1 = lo;
+    }
+    o0 = c0;
+    o1 = c1;
+}
+
+__host__ __device__ __forceinline__ uint32_t squares3_word(uint64_t key, uint64_t ctr)
+{
+    uint64_t x = key * ctr;
+    const uint64_t y = x;
+    const uint64_t z = y + key;
+    x = x * x + y; x = (x >> 32) | (x << 32);
+    x = x * x + z; x = (x >> 32) | (x << 32);
+    return static_cast<uint32_t>((x * x + y) >> 32);
+}
+
+// Number of uniforms one event draws: N-2 invariant masses + 2(N-1) angles.
+template <int N> struct Draws { static constexpr int value = 3 * N - 4; };
+
+// All raw words of event `evt` (zero-extended for squares3).
+template <int N, int ENGINE>
+__device__ __forceinline__ void event_words(uint64_t key, uint64_t evt, uint64_t (&w)[3 * N - 4])
+{
+    constexpr int NW = 3 * N - 4;
+    const uint64_t base = evt + 3u * N;   // state after discard(evt + 3N), size_t arithmetic
+    if constexpr (ENGINE == kPhilox) {
+        constexpr int NB = (NW + 1) / 2;
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+            const uint64_t c0 = base + 1u + b;
+            const uint64_t c1 = (c0 < base) ? 1u : 0u;     // carry of the 128-bit counter
+            uint64_t o0, o1;
+            philox2x64_7(c0, c1, key, o0, o1);
+            w[2 * b] = o0;
+            if (2 * b + 1 < NW) w[2 * b + 1] = o1;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < NW; ++k) w[k] = squares3_word(key, base + k);
+    }
+}
+
+template <int ENGINE>
+__device__ __forceinline__ double word_to_uniform(uint64_t x)
+{
+    if constexpr (ENGINE == kPhilox) return __ull2double_rn(x) * 0x1p-64;
+    else return static_cast<double>(static_cast<uint32_t>(x)) * 0x1p-32;
+}
+
+// Compare-exchange on raw words: the uniform map is monotone, so sorting the
+// words sorts the uniforms exactly as the reference's bubble sort of doubles
+// (DecayMother.h:128-151, 184) -- equal doubles are interchangeable.
+__device__ __forceinline__ void cswap(uint64_t& a, uint64_t& b)
+{
+    const uint64_t lo = a < b ? a : b;
+    const uint64_t hi = a < b ? b : a;
+    a = lo;
+    b = hi;
+}
+
+// Odd-even transposition network on w[0..K-1]; K <= 8 here.
+template <int K>
+__device__ __forceinline__ void sort_words(uint64_t* w)
+{
+#pragma unroll
+    for (int pass = 0; pass < K; ++pass) {
+#pragma unroll
+        for (int i = pass & 1; i + 1 < K; i += 2) cswap(w[i], w[i + 1]);
+    }
+}
+
+}  // namespace hps

@@ -1,0 +1,201 @@
+/*
+ * hps.h -- C ABI of the GB300-native phase-space generator (libhps.so).
+ *
+ * This is the drop-in seam for Hydra's phase-space hot path.  In Hydra the
+ * user calls hydra::PhaseSpace<N,GRND>::{Generate, AverageOn, Evaluate}; each
+ * builds a by-value functor {seed, ECM, max weight, beta, masses[N]} and hands
+ * it to exactly one Thrust algorithm through the launch helpers in
+ * hydra/detail/launch_decayers.inl:66-182.  Every entry point below replaces
+ * one of those launches (or a Decays member that walks the same storage); the
+ * reference line it replaces is cited beside it.  hps_channel carries the same
+ * scalars as the reference functor, computed on the host exactly as the
+ * reference constructor does (hps_channel_init).
+ *
+ * Conventions
+ *  - All calls are asynchronous on the given CUDA stream (cudaStream_t passed
+ *    as void*, NULL = legacy default stream) unless stated otherwise; inputs
+ *    and outputs are DEVICE pointers owned by the caller.  The library never
+ *    allocates an output.
+ *  - Event e of a call [first_evt, first_evt + n) is the reference's event
+ *    index first_evt + e: its random stream is the reference engine seeded
+ *    with channel.seed after discard(first_evt + e + 3N).
+ *  - Four-vectors are stored as Hydra's Decays does (hydra/Decays.h:72 and
+ *    hydra/multivector.h:70-108): one column per daughter, each column an
+ *    array of n Vector4R = {E, px, py, pz} doubles (32 bytes per event,
+ *    hydra/Vector4R.h:59,130).  Columns must be 32-byte aligned.
+ *  - Errors: every call returns hps_status; hps_last_error() gives a message
+ *    for the calling thread.  Where the reference throws, the status maps to
+ *    its exception (HPS_ERR_BAD_ARG -> std::invalid_argument,
+ *    HPS_ERR_NO_ENERGY -> std::runtime_error, HPS_ERR_CUDA -> thrust::system_error).
+ */
+#ifndef HPS_H_
+#define HPS_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HPS_MAX_DAUGHTERS 10
+#define HPS_ABI_VERSION 1
+
+typedef enum hps_status {
+    HPS_OK = 0,
+    HPS_ERR_BAD_ARG = 1,      /* invalid masses, N, pointers or sizes        */
+    HPS_ERR_NO_ENERGY = 2,    /* M - sum(m_i) <= 0                           */
+    HPS_ERR_OOM = 3,          /* a scratch allocation failed                 */
+    HPS_ERR_BUDGET = 4,       /* request above the admission budget          */
+    HPS_ERR_TIMEOUT = 5,      /* a bounded wait gave up                      */
+    HPS_ERR_CUDA = 6,         /* CUDA runtime error (message in last_error)  */
+    HPS_ERR_UNSUPPORTED = 7   /* combination not built into this library     */
+} hps_status;
+
+/* Random engines (template parameter GRND of hydra::PhaseSpace). */
+typedef enum hps_engine {
+    HPS_ENGINE_PHILOX = 0,    /* hydra::philox  = EngineR123<Philox2x64>, 7 rounds
+                                 (hydra/detail/random/EngineR123.h:244, hydra_R123/philox.h:266) */
+    HPS_ENGINE_SQUARES3 = 1   /* hydra::default_random_engine = squares3
+                                 (hydra/detail/PRNGTypedefs.h:59, random/squares3.h:67) */
+} hps_engine;
+
+/* Arithmetic of the kinematics.  FP64 follows the reference in IEEE double;
+ * FP32_FIX does rotations and boosts in float, keeping the threshold-sensitive
+ * pdk terms, the weight product and all reductions in double. */
+typedef enum hps_precision {
+    HPS_PREC_FP64 = 0,
+    HPS_PREC_FP32_FIX = 1
+} hps_precision;
+
+/* One decay channel: the scalars of hydra::detail::DecayMother
+ * (hydra/detail/functors/DecayMother.h:63-73). */
+typedef struct hps_channel {
+    int32_t n_daughters;                 /* N, 2..10                                   */
+    int32_t engine;                      /* hps_engine                                 */
+    uint64_t seed;                       /* size_t fSeed                               */
+    double ecm;                          /* fECM = M - sum(m_i)                        */
+    double max_weight;                   /* fMaxWeight = 1/prod PDK                    */
+    double beta[3];                      /* fBeta0..2, built as DecayMother.h:88-98    */
+    double masses[HPS_MAX_DAUGHTERS];    /* fMasses[N]                                 */
+} hps_channel;
+
+/* Per-event functor menu for AverageOn / Evaluate (arbitrary C++ functors
+ * cannot cross a C ABI; the C++ headers in include/hydra/ compile any functor
+ * into the kernel instead).
+ *   HPS_FN_ONE     f = 1
+ *   HPS_FN_MASS2   f = mass2(p_i + p_j)
+ *   HPS_FN_BW2     f = 1 / ((a^2 - mass2(p_i + p_j))^2 + (a b)^2),
+ *                  |relativistic Breit-Wigner|^2 with mass a and width b. */
+typedef enum hps_functor_kind { HPS_FN_ONE = 0, HPS_FN_MASS2 = 1, HPS_FN_BW2 = 2 } hps_functor_kind;
+
+typedef struct hps_functor {
+    int32_t kind;   /* hps_functor_kind */
+    int32_t i;
+    int32_t j;
+    int32_t reserved;
+    double a;
+    double b;
+} hps_functor;
+
+/* Weighted statistics of AverageOn: hydra::detail::StatsPHSP
+ * (hydra/detail/functors/StatsPHSP.h:38-59).  The reference returns
+ * (mean, sqrt(m2)/w) (hydra/detail/PhaseSpace.inl:271). */
+typedef struct hps_stats {
+    double mean;
+    double m2;
+    double w;
+} hps_stats;
+
+/* ---------------------------------------------------------------- set-up -- */
+
+/* Fills *ch as hydra::PhaseSpace<N,GRND>'s constructor (hydra/detail/PhaseSpace.inl:42-90)
+ * plus DecayMother's constructor (DecayMother.h:76-101) do.  mother = {E,px,py,pz}
+ * of the mother four-vector given to Generate (only the final-boost vector
+ * depends on it; ECM uses mother_mass, as in the reference).
+ * Returns HPS_ERR_BAD_ARG for a mass <= 0 or N outside 2..10, HPS_ERR_NO_ENERGY when
+ * M - sum(m_i) <= 0.  Host-only, synchronous. */
+hps_status hps_channel_init(hps_channel* ch, int32_t n_daughters, int32_t engine, uint64_t seed,
+                            double mother_mass, const double* masses, const double* mother);
+
+/* The reference's default seed when SetSeed is never called:
+ * 1 * (1 + hash_range(masses)) with std::hash<double> of the C++ standard library
+ * (hydra/detail/PhaseSpace.inl:44,64; hydra/detail/Hash.h:45-58). */
+uint64_t hps_default_seed(int32_t n_daughters, const double* masses);
+
+/* --------------------------------------------------------------- compute -- */
+
+/* Generate: replaces hydra::detail::launch_decayer -> thrust::tabulate(Decays, DecayMother)
+ * (hydra/detail/launch_decayers.inl:133-149, called from PhaseSpace.inl:351-394).
+ * cols[k] (host array of N device pointers) receives daughter k's Vector4R column.
+ * Optional outputs (NULL to skip):
+ *   weights[n]  generation-time event weight (the value DecayMother::process returns and
+ *               Generate discards, DecayMother.h:285; Evaluate's first column, EvalMother.h:305)
+ *   flags[n]    hit-or-miss flag of Decays::Unweight (hydra/detail/Decays.inl:75-89,415-455):
+ *               1 when PhaseSpaceWeight(p)/max_weight > u, u from squares3(unweight_seed)
+ *               after discard(first_evt + e). */
+hps_status hps_generate(const hps_channel* ch, uint64_t first_evt, uint64_t n,
+                        double* const* cols, double* weights, uint8_t* flags,
+                        uint64_t unweight_seed, int32_t precision, void* stream);
+
+/* Generate into HOST memory: the GPU form of Generate(mother, Decays<..., hydra::host::sys_t>)
+ * (PhaseSpace.inl:377-394 with a host-backend Decays).  Same outputs as hps_generate, but
+ * host_cols / host_weights / host_flags are host pointers (pinned memory gives full link
+ * bandwidth).  Events are produced in chunks of chunk_events (0 = library default) into two
+ * device staging buffers taken from the stream-ordered allocator; each chunk's device->host
+ * copies run on a second stream while the next chunk is generated.  Returns when all copies
+ * are complete (synchronous, like the reference call). */
+hps_status hps_generate_host(const hps_channel* ch, uint64_t first_evt, uint64_t n,
+                             double* const* host_cols, double* host_weights, uint8_t* host_flags,
+                             uint64_t unweight_seed, int32_t precision, uint64_t chunk_events,
+                             void* stream);
+
+/* Evaluate: replaces launch_evaluator -> thrust::tabulate(multivector, EvalMother)
+ * (hydra/detail/launch_decayers.inl:66-72, PhaseSpace.inl:314-329): per event the
+ * tuple (w, f_1(p), ..., f_k(p)) as k+1 columns; weights[n] = w, out[f][n] = f_f(p). */
+hps_status hps_evaluate(const hps_channel* ch, uint64_t first_evt, uint64_t n,
+                        const hps_functor* functors, int32_t n_functors,
+                        double* weights, double* const* out, int32_t precision, void* stream);
+
+/* AverageOn: replaces launch_reducer -> thrust::transform_reduce(AverageMother, AddStatsPHSP)
+ * (hydra/detail/launch_decayers.inl:94-106, PhaseSpace.inl:255-273).  Storage-free:
+ * events are generated, weighted and reduced in registers.  The reduction tree is fixed
+ * by n alone (tiles of HPS_AVG_TILE events, merged pairwise), so the result is
+ * bit-identical for every launch shape.  *out (device pointer) receives {mean, M2, W}.
+ * Scratch: ceil(n / HPS_AVG_TILE) * 24 bytes; pass workspace/workspace_bytes (device
+ * memory, >= hps_average_on_workspace_size(n)) or workspace = NULL to let the library
+ * take it from the stream-ordered allocator (cudaMallocAsync) for the call. */
+#define HPS_AVG_TILE 4096
+size_t hps_average_on_workspace_size(uint64_t n);
+hps_status hps_average_on(const hps_channel* ch, uint64_t first_evt, uint64_t n,
+                          const hps_functor* functor, hps_stats* out, void* workspace,
+                          size_t workspace_bytes, int32_t precision, void* stream);
+
+/* PhaseSpaceWeight over stored events: replaces Events | Events.GetEventWeightFunctor()
+ * (hydra/Decays.h:235-239, hydra/detail/Decays.inl:215-231).  out[n] = max_weight *
+ * prod_i pdk(|R + p_i|, m_i, |R|). */
+hps_status hps_event_weights(int32_t n_daughters, const double* masses, double max_weight,
+                             uint64_t n, const double* const* cols, double* out, void* stream);
+
+/* Unweight flags over stored events: the tagger of Decays::Unweight()
+ * (hydra/detail/Decays.inl:75-89, 444-445): flags[e] = weight/max_weight > u(first_evt + e). */
+hps_status hps_unweight_flags(int32_t n_daughters, const double* masses, double max_weight,
+                              uint64_t n, const double* const* cols, uint64_t unweight_seed,
+                              uint64_t first_evt, uint8_t* flags, void* stream);
+
+/* Raw random words of each event's stream (parity instrument): out[e*(3N-4)+k] is the k-th
+ * word the reference engine returns for event first_evt+e (EngineR123.h:149-166 returns 64-bit
+ * Philox words; squares3.h:105-119 returns 32-bit words, stored zero-extended). */
+hps_status hps_rng_words(int32_t n_daughters, int32_t engine, uint64_t seed, uint64_t first_evt,
+                         uint64_t n, uint64_t* out, void* stream);
+
+/* ------------------------------------------------------------------ misc -- */
+
+const char* hps_last_error(void);
+int32_t hps_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HPS_H_ */

@@ -1,0 +1,326 @@
+/*
+ * ref_harness.cpp -- test infrastructure, NOT product code.
+ *
+ * A command-line driver over the UNMODIFIED Hydra headers (hydra::PhaseSpace,
+ * hydra::Decays, hydra::PhaseSpaceWeight, hydra::random engines).  It is built
+ * by oracle/build_ref.sh straight from the Hydra source tree, with the cpp
+ * (sequential) or omp backend, and its outputs pin the C restatement in
+ * oracle/genbod_oracle.c and the golden fixtures under tests/golden/.
+ *
+ * Reference calls exercised (paths inside the Hydra project):
+ *   hydra/detail/PhaseSpace.inl:42-90      ctor: ECM, max weight, default seed
+ *   hydra/detail/PhaseSpace.inl:377-394    Generate(mother, Decays&)
+ *   hydra/detail/PhaseSpace.inl:255-273    AverageOn(policy, mother, functor, n)
+ *   hydra/detail/PhaseSpace.inl:314-329    Evaluate(mother, result, functor)
+ *   hydra/detail/Decays.inl:215-231        PhaseSpaceWeight::Evaluate (recomputed weight)
+ *   hydra/detail/Decays.inl:75-89          FlagDaugthers (hit-or-miss flag)
+ *   hydra/detail/Decays.inl:415-455        Decays::Unweight()
+ *   hydra/detail/random/EngineR123.h:97-172, squares3.h:105-125  raw RNG words
+ *
+ * Usage:
+ *   ref_harness rng  N engine seed n                      out.bin
+ *   ref_harness gen  N engine seed n M m0..m{N-1} fsel fi fj fa fb useed mx my mz out.bin
+ *   ref_harness avg  N engine seed n M m0..m{N-1} fsel fi fj fa fb out.bin
+ *   ref_harness time N engine seed n M m0..m{N-1} fsel fi fj fa fb reps
+ * engine: 0 = hydra::philox (Philox2x64, 7 rounds), 1 = hydra::default_random_engine (squares3)
+ * fsel:   0 = constant 1, 1 = mass2(p_i+p_j), 2 = 1/((a^2 - mass2(p_i+p_j))^2 + (a*b)^2)
+ * seed:   gen/avg/time: passed to PhaseSpace::SetSeed(GInt_t), -1 keeps the default (hash) seed;
+ *         rng: the raw 64-bit engine seed.
+ */
+#include <hydra/Types.h>
+#include <hydra/Vector4R.h>
+#include <hydra/PhaseSpace.h>
+#include <hydra/Decays.h>
+#include <hydra/Lambda.h>
+#include <hydra/Tuple.h>
+#include <hydra/multivector.h>
+#include <hydra/host/System.h>
+#include <hydra/device/System.h>
+#include <hydra/detail/random/EngineR123.h>
+#include <hydra/detail/random/squares3.h>
+
+#include <array>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+declarg(D0, hydra::Vector4R)
+declarg(D1, hydra::Vector4R)
+declarg(D2, hydra::Vector4R)
+declarg(D3, hydra::Vector4R)
+declarg(D4, hydra::Vector4R)
+declarg(D5, hydra::Vector4R)
+declarg(D6, hydra::Vector4R)
+declarg(D7, hydra::Vector4R)
+declarg(D8, hydra::Vector4R)
+declarg(D9, hydra::Vector4R)
+
+declarg(WCol, double)
+declarg(FCol, double)
+
+using namespace hydra::arguments;
+
+namespace {
+
+template <size_t N> struct ptypes;
+template <> struct ptypes<2>  { typedef hydra::tuple<D0, D1> type; };
+template <> struct ptypes<3>  { typedef hydra::tuple<D0, D1, D2> type; };
+template <> struct ptypes<4>  { typedef hydra::tuple<D0, D1, D2, D3> type; };
+template <> struct ptypes<5>  { typedef hydra::tuple<D0, D1, D2, D3, D4> type; };
+template <> struct ptypes<6>  { typedef hydra::tuple<D0, D1, D2, D3, D4, D5> type; };
+template <> struct ptypes<7>  { typedef hydra::tuple<D0, D1, D2, D3, D4, D5, D6> type; };
+template <> struct ptypes<8>  { typedef hydra::tuple<D0, D1, D2, D3, D4, D5, D6, D7> type; };
+template <> struct ptypes<9>  { typedef hydra::tuple<D0, D1, D2, D3, D4, D5, D6, D7, D8> type; };
+template <> struct ptypes<10> { typedef hydra::tuple<D0, D1, D2, D3, D4, D5, D6, D7, D8, D9> type; };
+
+struct FSpec { int sel; int i; int j; double a; double b; };
+
+// Scalar form of the functor menu; every implementation in this project
+// (C oracle, CUDA kernels) evaluates the same expression.
+inline double fmenu(FSpec const& f, hydra::Vector4R const* p)
+{
+    if (f.sel == 0) return 1.0;
+    hydra::Vector4R s = p[f.i] + p[f.j];
+    double m2 = s.mass2();
+    if (f.sel == 1) return m2;
+    double d = f.a * f.a - m2;
+    double g = f.a * f.b;
+    return 1.0 / (d * d + g * g);
+}
+
+#define HV hydra::Vector4R
+#define LAM_ARGS_2  HV p0, HV p1
+#define LAM_ARGS_3  LAM_ARGS_2, HV p2
+#define LAM_ARGS_4  LAM_ARGS_3, HV p3
+#define LAM_ARGS_5  LAM_ARGS_4, HV p4
+#define LAM_ARGS_6  LAM_ARGS_5, HV p5
+#define LAM_ARGS_7  LAM_ARGS_6, HV p6
+#define LAM_ARGS_8  LAM_ARGS_7, HV p7
+#define LAM_ARGS_9  LAM_ARGS_8, HV p8
+#define LAM_ARGS_10 LAM_ARGS_9, HV p9
+#define LAM_NAMES_2  p0, p1
+#define LAM_NAMES_3  LAM_NAMES_2, p2
+#define LAM_NAMES_4  LAM_NAMES_3, p3
+#define LAM_NAMES_5  LAM_NAMES_4, p4
+#define LAM_NAMES_6  LAM_NAMES_5, p5
+#define LAM_NAMES_7  LAM_NAMES_6, p6
+#define LAM_NAMES_8  LAM_NAMES_7, p7
+#define LAM_NAMES_9  LAM_NAMES_8, p8
+#define LAM_NAMES_10 LAM_NAMES_9, p9
+
+template <size_t N> struct menu_lambda;
+#define MENU_LAMBDA(NN)                                                        \
+    template <> struct menu_lambda<NN> {                                       \
+        static auto make(FSpec f) {                                            \
+            return hydra::wrap_lambda([f](LAM_ARGS_##NN) {                     \
+                HV arr[NN] = {LAM_NAMES_##NN};                                 \
+                return fmenu(f, arr);                                          \
+            });                                                                \
+        }                                                                      \
+    };
+MENU_LAMBDA(2) MENU_LAMBDA(3) MENU_LAMBDA(4) MENU_LAMBDA(5) MENU_LAMBDA(6)
+MENU_LAMBDA(7) MENU_LAMBDA(8) MENU_LAMBDA(9) MENU_LAMBDA(10)
+
+template <typename T>
+void write_bin(const char* path, std::vector<T> const& v)
+{
+    FILE* fp = std::fopen(path, "wb");
+    if (!fp) { std::perror(path); std::exit(3); }
+    if (!v.empty() && std::fwrite(v.data(), sizeof(T), v.size(), fp) != v.size()) {
+        std::perror("fwrite"); std::exit(3);
+    }
+    std::fclose(fp);
+}
+
+struct Args {
+    std::string mode;
+    int N = 0, engine = 0;
+    long long seed = 0;
+    size_t n = 0;
+    double M = 0;
+    double m[10] = {0};
+    FSpec f{0, 0, 1, 0.0, 0.0};
+    unsigned long long useed = 0x180ec6d33cfd0abaULL;
+    double mom[3] = {0, 0, 0};
+    const char* out = nullptr;
+    int reps = 1;
+};
+
+template <size_t N, typename GRND>
+void run_rng(Args const& a)
+{
+    const size_t nw = 3 * N - 4;
+    std::vector<unsigned long long> words(a.n * nw);
+    for (size_t evt = 0; evt < a.n; ++evt) {
+        GRND eng(static_cast<size_t>(a.seed));
+        eng.discard(evt + 3 * N);
+        for (size_t k = 0; k < nw; ++k) words[evt * nw + k] = eng();
+    }
+    write_bin(a.out, words);
+}
+
+template <size_t N, typename GRND>
+hydra::PhaseSpace<N, GRND> make_phsp(Args const& a)
+{
+    double masses[N];
+    for (size_t i = 0; i < N; ++i) masses[i] = a.m[i];
+    hydra::PhaseSpace<N, GRND> phsp(a.M, masses);
+    if (a.seed != -1) phsp.SetSeed(static_cast<hydra::GInt_t>(a.seed));
+    return phsp;
+}
+
+template <size_t N, typename GRND>
+void run_gen(Args const& a)
+{
+    typedef typename ptypes<N>::type PT;
+    auto phsp = make_phsp<N, GRND>(a);
+    double masses[N];
+    for (size_t i = 0; i < N; ++i) masses[i] = a.m[i];
+    double E = std::sqrt(a.M * a.M + a.mom[0] * a.mom[0] + a.mom[1] * a.mom[1] + a.mom[2] * a.mom[2]);
+    hydra::Vector4R mother(E, a.mom[0], a.mom[1], a.mom[2]);
+
+    hydra::Decays<PT, hydra::host::sys_t> events(a.M, masses, a.n);
+    phsp.Generate(mother, events);
+
+    auto functor = menu_lambda<N>::make(a.f);
+    hydra::multivector<hydra::tuple<WCol, FCol>, hydra::host::sys_t> evals(a.n);
+    phsp.Evaluate(mother, evals, functor);
+
+    auto wfun = events.GetEventWeightFunctor();
+    typedef hydra::detail::FlagDaugthers<decltype(wfun)> tagger_t;
+    tagger_t tagger(wfun, events.GetMaxWeight(), static_cast<size_t>(a.useed));
+
+    // layout: [n*N*4 four-vectors][n gen weights][n functor values]
+    //         [n recomputed weights][n flags][maxW_phsp, maxW_decays, ECM, seed, n_unweighted,
+    //          default-seed bits]
+    std::vector<double> out;
+    out.reserve(a.n * (4 * N + 4) + 5);
+    for (size_t i = 0; i < a.n; ++i) {
+        auto ev = events[i];
+        hydra::Vector4R p[N];
+        hydra::detail::assignTupleToArray(ev, p);
+        for (size_t k = 0; k < N; ++k)
+            for (int c = 0; c < 4; ++c) out.push_back(p[k].get(c));
+    }
+    for (size_t i = 0; i < a.n; ++i) out.push_back(hydra::get<0>(evals[i]));
+    for (size_t i = 0; i < a.n; ++i) out.push_back(hydra::get<1>(evals[i]));
+    for (size_t i = 0; i < a.n; ++i) out.push_back(wfun(events[i]));
+    for (size_t i = 0; i < a.n; ++i)
+        out.push_back(tagger(hydra::make_tuple(i, events[i])) ? 1.0 : 0.0);
+    out.push_back(phsp.GetMaxWeight());
+    out.push_back(events.GetMaxWeight());
+    out.push_back(phsp.GetECM());
+    out.push_back(static_cast<double>(phsp.GetSeed()));
+    auto kept = events.Unweight(static_cast<size_t>(a.useed));
+    out.push_back(static_cast<double>(kept.size()));
+    // default seed of the constructor (PhaseSpace.inl:44,64), bit pattern stored in a double slot
+    size_t dseed = 1;
+    dseed *= (1 + hydra::detail::hash_range(&masses[0], &masses[0] + N));
+    double dbits;
+    std::memcpy(&dbits, &dseed, sizeof(dbits));
+    out.push_back(dbits);
+    write_bin(a.out, out);
+}
+
+template <size_t N, typename GRND>
+void run_avg(Args const& a)
+{
+    auto phsp = make_phsp<N, GRND>(a);
+    hydra::Vector4R mother(a.M, 0.0, 0.0, 0.0);
+    auto functor = menu_lambda<N>::make(a.f);
+    auto r = phsp.AverageOn(hydra::device::sys, mother, functor, a.n);
+    std::vector<double> out{r.first, r.second};
+    write_bin(a.out, out);
+}
+
+template <size_t N, typename GRND>
+void run_time(Args const& a)
+{
+    typedef typename ptypes<N>::type PT;
+    auto phsp = make_phsp<N, GRND>(a);
+    double masses[N];
+    for (size_t i = 0; i < N; ++i) masses[i] = a.m[i];
+    hydra::Vector4R mother(a.M, 0.0, 0.0, 0.0);
+    auto functor = menu_lambda<N>::make(a.f);
+    hydra::Decays<PT, hydra::device::sys_t> events(a.M, masses, a.n);
+    double best_gen = 1e30, best_avg = 1e30;
+    for (int r = 0; r < a.reps; ++r) {
+        auto t0 = std::chrono::steady_clock::now();
+        phsp.Generate(mother, events);
+        auto t1 = std::chrono::steady_clock::now();
+        auto s = phsp.AverageOn(hydra::device::sys, mother, functor, a.n);
+        auto t2 = std::chrono::steady_clock::now();
+        (void)s;
+        best_gen = std::min(best_gen, std::chrono::duration<double>(t1 - t0).count());
+        best_avg = std::min(best_avg, std::chrono::duration<double>(t2 - t1).count());
+    }
+    std::printf("{\"n\": %zu, \"N\": %zu, \"generate_s\": %.6f, \"average_s\": %.6f}\n",
+                a.n, N, best_gen, best_avg);
+}
+
+template <size_t N, typename GRND>
+void dispatch_mode(Args const& a)
+{
+    if (a.mode == "rng") run_rng<N, GRND>(a);
+    else if (a.mode == "gen") run_gen<N, GRND>(a);
+    else if (a.mode == "avg") run_avg<N, GRND>(a);
+    else if (a.mode == "time") run_time<N, GRND>(a);
+    else { std::fprintf(stderr, "unknown mode %s\n", a.mode.c_str()); std::exit(2); }
+}
+
+template <size_t N>
+void dispatch_engine(Args const& a)
+{
+    if (a.engine == 0) dispatch_mode<N, hydra::philox>(a);
+    else dispatch_mode<N, hydra::default_random_engine>(a);
+}
+
+} // namespace
+
+int main(int argc, char** argv)
+{
+    if (argc < 6) { std::fprintf(stderr, "see header for usage\n"); return 2; }
+    Args a;
+    int k = 1;
+    a.mode = argv[k++];
+    a.N = std::atoi(argv[k++]);
+    a.engine = std::atoi(argv[k++]);
+    {
+        const char* sarg = argv[k++];
+        a.seed = (sarg[0] == '-') ? std::strtoll(sarg, nullptr, 0)
+                                  : static_cast<long long>(std::strtoull(sarg, nullptr, 0));
+    }
+    a.n = std::strtoull(argv[k++], nullptr, 0);
+    if (a.N < 2 || a.N > 10) { std::fprintf(stderr, "N out of range\n"); return 2; }
+    if (a.mode != "rng") {
+        if (argc < k + 1 + a.N + 5) { std::fprintf(stderr, "missing args\n"); return 2; }
+        a.M = std::strtod(argv[k++], nullptr);
+        for (int i = 0; i < a.N; ++i) a.m[i] = std::strtod(argv[k++], nullptr);
+        a.f.sel = std::atoi(argv[k++]);
+        a.f.i = std::atoi(argv[k++]);
+        a.f.j = std::atoi(argv[k++]);
+        a.f.a = std::strtod(argv[k++], nullptr);
+        a.f.b = std::strtod(argv[k++], nullptr);
+        if (a.mode == "gen") {
+            a.useed = std::strtoull(argv[k++], nullptr, 0);
+            for (int c = 0; c < 3; ++c) a.mom[c] = std::strtod(argv[k++], nullptr);
+        }
+    }
+    if (a.mode == "time") a.reps = (k < argc) ? std::atoi(argv[k++]) : 3;
+    else a.out = (k < argc) ? argv[k++] : "out.bin";
+    switch (a.N) {
+    case 2: dispatch_engine<2>(a); break;
+    case 3: dispatch_engine<3>(a); break;
+    case 4: dispatch_engine<4>(a); break;
+    case 5: dispatch_engine<5>(a); break;
+    case 6: dispatch_engine<6>(a); break;
+    case 7: dispatch_engine<7>(a); break;
+    case 8: dispatch_engine<8>(a); break;
+    case 9: dispatch_engine<9>(a); break;
+    case 10: dispatch_engine<10>(a); break;
+    }
+    return 0;
+}

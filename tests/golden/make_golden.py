@@ -1,0 +1,103 @@
+"""Regenerates the golden fixtures in this directory from the REFERENCE itself.
+
+Runs oracle/_ref/ref_harness_cpp (Hydra's own PhaseSpace / Decays / engines,
+built by oracle/build_ref.sh with the sequential cpp backend and
+-ffp-contract=off) on small seeded cases and stores its outputs as .npz.
+Needs the Hydra source tree, so it runs only where that tree exists; the
+fixtures it writes are committed and read by tests/test_oracle_golden.py and
+tests/test_gpu_parity.py.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import subprocess
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parent.parent
+REF = REPO / "oracle" / "_ref" / "ref_harness_cpp"
+UNWEIGHT_SEED = 0x180EC6D33CFD0ABA   # hydra/Decays.h:253 default
+
+PI = 0.13957
+K = 0.493677
+# (name, N, engine, seed, n, M, masses, functor(sel,i,j,a,b), mother momentum)
+GEN_CASES = [
+    ("cfg1_n3_philox", 3, 0, 0x3039, 256, 5.27934, [3.0969, K, PI], (1, 0, 1, 0.0, 0.0), (0, 0, 0)),
+    ("cfg2_n5_philox", 5, 0, 0x3039, 256, 1.86484, [K, PI, PI, PI, PI], (2, 0, 1, 0.8955, 0.0473),
+     (0, 0, 0)),
+    ("cfg3_n10_philox", 10, 0, 0x3039, 128, 5.0, [PI] * 10, (2, 0, 1, 0.8955, 0.0473), (0, 0, 0)),
+    ("n2_philox", 2, 0, 7, 64, 1.0, [0.2, 0.3], (1, 0, 1, 0.0, 0.0), (0, 0, 0)),
+    ("n4_squares3", 4, 1, 12345, 128, 3.0, [0.1, 0.2, 0.3, 0.4], (1, 1, 3, 0.0, 0.0), (0, 0, 0)),
+    ("n7_squares3", 7, 1, 99, 96, 4.0, [PI] * 4 + [K, 0.938272, PI], (2, 2, 5, 1.0, 0.1), (0, 0, 0)),
+    ("n6_philox_moving", 6, 0, 2024, 64, 3.5, [PI, K, PI, K, PI, 0.2], (1, 0, 5, 0.0, 0.0),
+     (0.3, -1.2, 0.7)),
+    ("n3_philox_defaultseed", 3, 0, -1, 64, 5.27934, [3.0969, K, PI], (0, 0, 1, 0.0, 0.0), (0, 0, 0)),
+    ("n8_philox_threshold", 8, 0, 31337, 128, 8 * PI + 0.01, [PI] * 8, (1, 0, 7, 0.0, 0.0), (0, 0, 0)),
+]
+# (name, N, engine, seed, n)
+RNG_CASES = [
+    ("rng_n3_philox", 3, 0, 0x3039, 64),
+    ("rng_n5_philox", 5, 0, 0x3039, 64),
+    ("rng_n10_philox", 10, 0, 0xDEADBEEFCAFEF00D, 48),
+    ("rng_n5_squares3", 5, 1, 0x3039, 64),
+    ("rng_n2_squares3", 2, 1, 1, 16),
+]
+# (name, N, engine, seed, n, M, masses, functor)
+AVG_CASES = [
+    ("avg_cfg1_m2", 3, 0, 0x3039, 20000, 5.27934, [3.0969, K, PI], (1, 0, 1, 0.0, 0.0)),
+    ("avg_cfg2_bw", 5, 0, 0x3039, 20000, 1.86484, [K, PI, PI, PI, PI], (2, 0, 1, 0.8955, 0.0473)),
+    ("avg_n10_bw", 10, 0, 0x3039, 5000, 5.0, [PI] * 10, (2, 0, 1, 0.8955, 0.0473)),
+    ("avg_n4_sq_one", 4, 1, 12345, 5000, 3.0, [0.1, 0.2, 0.3, 0.4], (0, 0, 1, 0.0, 0.0)),
+]
+
+
+def run(args, out):
+    subprocess.run([str(REF)] + [str(a) for a in args] + [str(out)], check=True)
+    return out
+
+
+def fnum(x):
+    return repr(float(x))
+
+
+def main():
+    if not REF.exists():
+        sys.exit(f"{REF} missing: run oracle/build_ref.sh first")
+    tmp = HERE / "_tmp.bin"
+    fixtures = {}
+    for name, N, eng, seed, n, M, m, f, mom in GEN_CASES:
+        args = ["gen", N, eng, seed, n, fnum(M)] + [fnum(x) for x in m] + \
+               [f[0], f[1], f[2], fnum(f[3]), fnum(f[4]), hex(UNWEIGHT_SEED)] + [fnum(x) for x in mom]
+        d = np.fromfile(run(args, tmp), dtype=np.float64)
+        o = n * N * 4
+        E = float(np.sqrt(M * M + sum(x * x for x in mom)))
+        fixtures[name] = dict(
+            N=N, engine=eng, seed=seed, n=n, M=M, masses=np.array(m), functor=np.array(f),
+            mother=np.array([E, *mom]), useed=np.uint64(UNWEIGHT_SEED),
+            four=d[:o].reshape(n, N, 4).transpose(1, 0, 2).copy(),
+            w_gen=d[o:o + n], f_val=d[o + n:o + 2 * n], w_rec=d[o + 2 * n:o + 3 * n],
+            flags=d[o + 3 * n:o + 4 * n].astype(np.uint8),
+            max_weight=d[o + 4 * n], decays_max_weight=d[o + 4 * n + 1], ecm=d[o + 4 * n + 2],
+            get_seed=d[o + 4 * n + 3], n_unweighted=d[o + 4 * n + 4],
+            default_seed=d[o + 4 * n + 5:o + 4 * n + 6].view(np.uint64)[0])
+    for name, N, eng, seed, n in RNG_CASES:
+        d = np.fromfile(run(["rng", N, eng, seed, n], tmp), dtype=np.uint64)
+        fixtures[name] = dict(N=N, engine=eng, seed=np.uint64(seed), n=n, words=d.reshape(n, 3 * N - 4))
+    for name, N, eng, seed, n, M, m, f in AVG_CASES:
+        args = ["avg", N, eng, seed, n, fnum(M)] + [fnum(x) for x in m] + \
+               [f[0], f[1], f[2], fnum(f[3]), fnum(f[4])]
+        d = np.fromfile(run(args, tmp), dtype=np.float64)
+        fixtures[name] = dict(N=N, engine=eng, seed=seed, n=n, M=M, masses=np.array(m),
+                              functor=np.array(f), mean=d[0], err=d[1])
+    tmp.unlink()
+    for name, fx in fixtures.items():
+        np.savez_compressed(HERE / f"{name}.npz", **fx)
+    print(f"wrote {len(fixtures)} fixtures to {HERE}")
+
+
+if __name__ == "__main__":
+    main()

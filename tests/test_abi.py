@@ -1,0 +1,115 @@
+"""C ABI checks that need no GPU: the library builds, loads and exports every symbol
+include/*.h declares; host-side set-up (hps_channel_init, default seed, workspace size)
+matches the reference fixtures; argument errors map to the reference's exceptions."""
+from __future__ import annotations
+
+import ctypes
+import re
+
+import numpy as np
+import pytest
+
+from conftest import GEN_GOLDEN, REPO, load_golden
+
+
+def declared_symbols():
+    syms = set()
+    for h in (REPO / "include").glob("*.h"):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(hps_\w+)\s*\(", text, flags=re.M):
+            syms.add(m.group(1))
+    return sorted(syms)
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    for s in ("hps_generate", "hps_average_on", "hps_evaluate", "hps_channel_init"):
+        assert s in syms
+
+
+def test_library_exports_every_declared_symbol(hps):
+    L = ctypes.CDLL(str(hps.library_path()))
+    missing = [s for s in declared_symbols() if not hasattr(L, s)]
+    assert not missing, missing
+    # the Python binding covers the same set
+    assert set(declared_symbols()) <= set(hps.SIGNATURES)
+
+
+def test_abi_version(hps):
+    assert hps.lib().hps_abi_version() == 1
+
+
+@pytest.mark.parametrize("name", GEN_GOLDEN)
+def test_channel_init_matches_reference(hps, name):
+    from hydra_gb300 import api
+    g = load_golden(name)
+    ch = api.make_channel(list(g["masses"]), float(g["M"]), 1, int(g["engine"]), list(g["mother"]))
+    assert ch.max_weight == g["max_weight"]
+    assert ch.ecm == g["ecm"]
+
+
+def test_default_seed_matches_reference(hps):
+    from hydra_gb300 import api
+    g = load_golden("n3_philox_defaultseed")
+    assert api.default_seed(list(g["masses"])) == int(g["default_seed"])
+    ps = api.PhaseSpace(float(g["M"]), list(g["masses"]), engine="philox")
+    assert ps.GetSeed() == int(g["get_seed"])
+
+
+def test_seed_is_gint(hps):
+    from hydra_gb300 import api
+    ps = api.PhaseSpace(5.27934, [3.0969, 0.493677, 0.13957], engine="philox")
+    ps.SetSeed(0x3039)
+    assert ps.GetSeed() == 12345
+    ps.SetSeed(-5)
+    assert ps.GetSeed() == -5 and ps._seed == 2**64 - 5      # sign-extended into size_t
+    ps.SetSeed(2**32 + 7)
+    assert ps.GetSeed() == 7
+
+
+def test_channel_errors_map_to_reference_exceptions(hps):
+    from hydra_gb300 import api
+    with pytest.raises(ValueError, match="daughter particle"):
+        api.make_channel([0.1, 0.0], 1.0, 1)
+    with pytest.raises(ValueError, match="mother particle"):
+        api.make_channel([0.1, 0.2], -1.0, 1)
+    with pytest.raises(RuntimeError, match="Not enough energy"):
+        api.make_channel([0.6, 0.5], 1.0, 1)
+    with pytest.raises(ValueError):
+        api.make_channel([0.1], 1.0, 1)
+    with pytest.raises(ValueError):
+        api.make_channel([0.1] * 11, 5.0, 1)
+
+
+def test_workspace_size(hps):
+    from hydra_gb300 import api
+    assert api.average_on_workspace_size(0) == 24
+    assert api.average_on_workspace_size(1) == 24
+    assert api.average_on_workspace_size(4096) == 24
+    assert api.average_on_workspace_size(4097) == 48
+    assert api.average_on_workspace_size(2**24) == 24 * 4096
+
+
+def test_bad_arguments_rejected_before_launch(hps):
+    """Validation happens on the host: no device is touched for these calls."""
+    lib = hps.lib()
+    ch = hps.HpsChannel()
+    ch.n_daughters = 11
+    st = lib.hps_generate(ctypes.byref(ch), 0, 10, None, None, None, 0, 0, None)
+    assert st == hps.ERR_BAD_ARG
+    assert b"outside 2..10" in lib.hps_last_error()
+    from hydra_gb300 import api
+    ch = api.make_channel([0.1, 0.2, 0.3], 1.0, 1)
+    st = lib.hps_generate(ctypes.byref(ch), 2**64 - 5, 10, None, None, None, 0, 0, None)
+    assert st == hps.ERR_BAD_ARG and b"wraps" in lib.hps_last_error()
+    st = lib.hps_generate(ctypes.byref(ch), 0, 10, None, None, None, 0, 7, None)
+    assert st == hps.ERR_BAD_ARG
+    cols = (ctypes.c_void_p * 3)(8, 16, 32)      # misaligned column 0, never dereferenced
+    st = lib.hps_generate(ctypes.byref(ch), 0, 10, ctypes.cast(cols, ctypes.c_void_p), None, None, 0, 0, None)
+    assert st == hps.ERR_BAD_ARG and b"aligned" in lib.hps_last_error()
+    fn = api.functor_mass2(0, 3)
+    out = ctypes.c_void_p(64)
+    st = lib.hps_average_on(ctypes.byref(ch), 0, 10, ctypes.byref(fn), out, None, 0, 0, None)
+    assert st == hps.ERR_BAD_ARG and b"indices" in lib.hps_last_error()
+    # n == 0 is a no-op, as an empty Thrust range
+    assert lib.hps_generate(ctypes.byref(ch), 0, 0, None, None, None, 0, 0, None) == hps.OK
