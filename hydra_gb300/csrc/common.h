@@ -8,6 +8,7 @@
 
 #include "../../include/hps.h"
 #include "genbod.cuh"
+#include "genbod_f32.cuh"
 
 namespace hps {
 
@@ -24,8 +25,19 @@ inline hps_status cuda_status(cudaError_t e, const char* what)
 // Validates the channel and converts it to the kernel-side form.
 hps_status to_device_channel(const hps_channel* ch, DevChannel* out);
 hps_status to_device_functor(const hps_functor* f, int n_daughters, DevFunctor* out);
+// Float-side constants for the FP32_FIX kernels (prefix sums formed in double, then rounded).
+void to_device_channel_f(const hps_channel* ch, DevChannelF* out);
 
-inline bool range_ok(uint64_t first, uint64_t n) { return first + n >= first; }
+// AverageOn pieces shared by its entry points (hps_average.cu): host-side validation that
+// touches no device state, and the tile + final-merge launches into caller-provided partials.
+hps_status average_args(const hps_channel* channel, const hps_functor* functor, int32_t precision,
+                        DevChannel* ch, DevFunctor* fn);
+hps_status launch_average(const hps_channel* channel, const DevChannel& ch, const DevFunctor& fn,
+                          uint64_t first_evt, uint64_t n, hps_stats* out, hps_stats* partials,
+                          int32_t precision, cudaStream_t stream);
+
+// Events [first, first + n) must not run past index 2^64 - 1.
+inline bool range_ok(uint64_t first, uint64_t n) { return n == 0 || first + (n - 1) >= first; }
 
 inline bool aligned(const void* p, size_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }
 

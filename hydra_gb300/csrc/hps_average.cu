@@ -43,6 +43,46 @@ k_average_tiles_f64(DevChannel ch, DevFunctor fn, uint64_t first, uint64_t n, ui
     }
 }
 
+// FP32_FIX form: the event (kinematics in float) and the functor value in float; each thread
+// accumulates its events as shifted weighted sums in double (W, sum w(f-K), sum w(f-K)^2 with K
+// its first value), which is the StatsPHSP of those events in closed form, then the same fixed
+// warp/CTA tree merges the per-thread StatsPHSP.
+template <int N, int ENGINE>
+__global__ void __launch_bounds__(kAvgThreads)
+k_average_tiles_f32fix(DevChannel chd, DevChannelF ch, DevFunctor fn, uint64_t first, uint64_t n,
+                       uint64_t ntiles, hps_stats* __restrict__ partials)
+{
+    for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        double sw = 0.0, s1 = 0.0, s2 = 0.0;
+        float K = 0.0f;
+        const uint64_t base = t * HPS_AVG_TILE + threadIdx.x;
+        for (int k = 0; k < kAvgPerThread; ++k) {
+            const uint64_t e = base + (uint64_t)k * kAvgThreads;
+            if (e < n) {
+                float p[N][4];
+                double prod;
+                const double w = f32::event<N, ENGINE>(chd, ch, first + e, p, prod);
+                const float f = f32::functor<N>(fn, p);
+                if (k == 0) K = f;
+                const double d = f32::widen(f - K);
+                const double wd = w * d;
+                sw += w;
+                s1 += wd;
+                s2 = fma(wd, d, s2);
+            }
+        }
+        hps_stats acc{0.0, 0.0, 0.0};
+        if (sw != 0.0) {
+            const double q = s1 / sw;
+            acc.w = sw;
+            acc.mean = f32::widen(K) + q;
+            acc.m2 = fma(-s1, q, s2);
+        }
+        const hps_stats r = block_reduce_stats<kAvgThreads>(acc);
+        if (threadIdx.x == 0) partials[t] = r;
+    }
+}
+
 // One CTA: thread j folds partials j, j+1024, ... in order, then the fixed CTA tree.
 __global__ void __launch_bounds__(kFinalThreads)
 k_average_final(const hps_stats* __restrict__ partials, uint64_t ntiles, hps_stats* __restrict__ out)
@@ -63,22 +103,31 @@ hps_status average_args(const hps_channel* channel, const hps_functor* functor, 
     if (st != HPS_OK) return st;
     if (precision != HPS_PREC_FP64 && precision != HPS_PREC_FP32_FIX)
         return set_error(HPS_ERR_BAD_ARG, "unknown precision %d", precision);
-    if (precision == HPS_PREC_FP32_FIX)
-        return set_error(HPS_ERR_UNSUPPORTED, "FP32_FIX average not built yet");
     return HPS_OK;
 }
 
 hps_status launch_average(const hps_channel* channel, const DevChannel& ch, const DevFunctor& fn,
                           uint64_t first_evt, uint64_t n, hps_stats* out, hps_stats* partials,
-                          cudaStream_t stream)
+                          int32_t precision, cudaStream_t stream)
 {
     const uint64_t ntiles = (n + HPS_AVG_TILE - 1) / HPS_AVG_TILE;
     if (ntiles > 0) {
         const unsigned grid = static_cast<unsigned>(ntiles < 152u * 16u ? ntiles : 152u * 16u);
-#define HPS_BODY(NN, EE)                                                                           \
-    k_average_tiles_f64<NN, EE><<<grid, kAvgThreads, 0, stream>>>(ch, fn, first_evt, n, ntiles, partials);
-        HPS_DISPATCH_N_ENGINE(channel->n_daughters, channel->engine, HPS_BODY)
+        if (precision == HPS_PREC_FP32_FIX) {
+            DevChannelF chf;
+            to_device_channel_f(channel, &chf);
+#define HPS_BODY(NN, EE)                                                                          \
+            k_average_tiles_f32fix<NN, EE><<<grid, kAvgThreads, 0, stream>>>(ch, chf, fn, first_evt, n, \
+                                                                              ntiles, partials);
+            HPS_DISPATCH_N_ENGINE(channel->n_daughters, channel->engine, HPS_BODY)
 #undef HPS_BODY
+        } else {
+#define HPS_BODY(NN, EE)                                                                          \
+            k_average_tiles_f64<NN, EE><<<grid, kAvgThreads, 0, stream>>>(ch, fn, first_evt, n, ntiles, \
+                                                                           partials);
+            HPS_DISPATCH_N_ENGINE(channel->n_daughters, channel->engine, HPS_BODY)
+#undef HPS_BODY
+        }
     }
     k_average_final<<<1, kFinalThreads, 0, stream>>>(partials, ntiles, out);
     return cuda_status(cudaGetLastError(), "hps_average_on launch");
@@ -113,7 +162,7 @@ hps_status hps_average_on(const hps_channel* channel, uint64_t first_evt, uint64
         if (workspace_bytes < need)
             return set_error(HPS_ERR_BAD_ARG, "workspace of %zu bytes, %zu needed", workspace_bytes, need);
         if (!aligned(workspace, 8)) return set_error(HPS_ERR_BAD_ARG, "workspace not 8-byte aligned");
-        return launch_average(channel, ch, fn, first_evt, n, out, static_cast<hps_stats*>(workspace), s);
+        return launch_average(channel, ch, fn, first_evt, n, out, static_cast<hps_stats*>(workspace), precision, s);
     }
     void* scratch = nullptr;
     cudaError_t e = cudaMallocAsync(&scratch, need, s);
@@ -121,7 +170,7 @@ hps_status hps_average_on(const hps_channel* channel, uint64_t first_evt, uint64
         cudaGetLastError();
         return set_error(HPS_ERR_OOM, "cudaMallocAsync(%zu): %s", need, cudaGetErrorString(e));
     }
-    st = launch_average(channel, ch, fn, first_evt, n, out, static_cast<hps_stats*>(scratch), s);
+    st = launch_average(channel, ch, fn, first_evt, n, out, static_cast<hps_stats*>(scratch), precision, s);
     e = cudaFreeAsync(scratch, s);
     if (st == HPS_OK && e != cudaSuccess) return cuda_status(e, "cudaFreeAsync");
     return st;

@@ -42,6 +42,20 @@ hps_status to_device_channel(const hps_channel* ch, DevChannel* out)
     return HPS_OK;
 }
 
+void to_device_channel_f(const hps_channel* ch, DevChannelF* out)
+{
+    std::memset(out, 0, sizeof(*out));
+    double S = 0.0;
+    for (int i = 0; i < ch->n_daughters; ++i) {
+        S += ch->masses[i];
+        out->m[i] = static_cast<float>(ch->masses[i]);
+        out->m2[i] = static_cast<float>(ch->masses[i] * ch->masses[i]);
+        out->S[i] = static_cast<float>(S);
+    }
+    out->ecm = static_cast<float>(ch->ecm);
+    out->ecm_2m64 = static_cast<float>(ch->ecm) * 0x1p-64f;
+}
+
 hps_status to_device_functor(const hps_functor* f, int n_daughters, DevFunctor* out)
 {
     if (!f) return set_error(HPS_ERR_BAD_ARG, "functor is NULL");

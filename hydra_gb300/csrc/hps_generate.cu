@@ -35,6 +35,34 @@ k_generate_f64(DevChannel ch, Cols cols, double* __restrict__ weights, uint8_t* 
     }
 }
 
+// FP32_FIX store path: kinematics in float (light-cone boosts, exact-octant angles),
+// weight and unweight test in double; four-vectors widened to double for the Decays columns.
+// The unweight flag compares prod(pdk) -- weight / max_weight, the quantity FlagDaugthers
+// tests -- with u, using the generation-time weight.
+template <int N, int ENGINE>
+__global__ void __launch_bounds__(256)
+k_generate_f32fix(DevChannel chd, DevChannelF ch, Cols cols, double* __restrict__ weights,
+                  uint8_t* __restrict__ flags, uint64_t ukey, uint64_t first, uint64_t n, int vec32)
+{
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < n;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        float p[N][4];
+        double prod;
+        const double wt = f32::event<N, ENGINE>(chd, ch, first + e, p, prod);
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            const double v[4] = {f32::widen(p[k][0]), f32::widen(p[k][1]), f32::widen(p[k][2]),
+                                 f32::widen(p[k][3])};
+            store_vec4(cols.p[k], e, v, vec32 != 0);
+        }
+        if (weights) weights[e] = wt;
+        if (flags) {
+            const double u = static_cast<double>(squares3_word(ukey, first + e)) * 0x1p-32;
+            flags[e] = (prod > u) ? 1 : 0;
+        }
+    }
+}
+
 constexpr int kMaxFunctors = 8;
 struct Functors { DevFunctor f[kMaxFunctors]; };
 struct OutCols { double* p[kMaxFunctors]; };
@@ -50,6 +78,21 @@ k_evaluate_f64(DevChannel ch, Functors fs, int nf, double* __restrict__ weights,
         const double wt = f64::event<N, ENGINE>(ch, first + e, p);
         if (weights) weights[e] = wt;
         for (int k = 0; k < nf; ++k) out.p[k][e] = functor_f64<N>(fs.f[k], p);
+    }
+}
+
+template <int N, int ENGINE>
+__global__ void __launch_bounds__(256)
+k_evaluate_f32fix(DevChannel chd, DevChannelF ch, Functors fs, int nf, double* __restrict__ weights,
+                  OutCols out, uint64_t first, uint64_t n)
+{
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < n;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        float p[N][4];
+        double prod;
+        const double wt = f32::event<N, ENGINE>(chd, ch, first + e, p, prod);
+        if (weights) weights[e] = wt;
+        for (int k = 0; k < nf; ++k) out.p[k][e] = f32::widen(f32::functor<N>(fs.f[k], p));
     }
 }
 
@@ -82,16 +125,24 @@ hps_status hps_generate(const hps_channel* channel, uint64_t first_evt, uint64_t
         cc.p[k] = cols[k];
     }
     if (weights && !aligned(weights, 8)) return set_error(HPS_ERR_BAD_ARG, "weights not 8-byte aligned");
-    if (precision == HPS_PREC_FP32_FIX)
-        return set_error(HPS_ERR_UNSUPPORTED, "FP32_FIX generate not built yet");
     const uint64_t ukey = splitmix64(unweight_seed);
     const unsigned grid = grid_for(n, 256);
     const int vec32 = all32 ? 1 : 0;
-#define HPS_BODY(NN, EE)                                                                  \
-    k_generate_f64<NN, EE><<<grid, 256, 0, as_stream(stream)>>>(ch, cc, weights, flags, ukey, \
-                                                                 first_evt, n, vec32);
-    HPS_DISPATCH_N_ENGINE(N, channel->engine, HPS_BODY)
+    if (precision == HPS_PREC_FP32_FIX) {
+        DevChannelF chf;
+        to_device_channel_f(channel, &chf);
+#define HPS_BODY(NN, EE)                                                                         \
+        k_generate_f32fix<NN, EE><<<grid, 256, 0, as_stream(stream)>>>(ch, chf, cc, weights, flags, ukey, \
+                                                                        first_evt, n, vec32);
+        HPS_DISPATCH_N_ENGINE(N, channel->engine, HPS_BODY)
 #undef HPS_BODY
+    } else {
+#define HPS_BODY(NN, EE)                                                                  \
+        k_generate_f64<NN, EE><<<grid, 256, 0, as_stream(stream)>>>(ch, cc, weights, flags, ukey, \
+                                                                     first_evt, n, vec32);
+        HPS_DISPATCH_N_ENGINE(N, channel->engine, HPS_BODY)
+#undef HPS_BODY
+    }
     return cuda_status(cudaGetLastError(), "hps_generate launch");
 }
 
@@ -117,14 +168,22 @@ hps_status hps_evaluate(const hps_channel* channel, uint64_t first_evt, uint64_t
         if (!out || !out[k]) return set_error(HPS_ERR_BAD_ARG, "output column %d is NULL", k);
         oc.p[k] = out[k];
     }
-    if (precision == HPS_PREC_FP32_FIX)
-        return set_error(HPS_ERR_UNSUPPORTED, "FP32_FIX evaluate not built yet");
     const unsigned grid = grid_for(n, 256);
-#define HPS_BODY(NN, EE)                                                                          \
-    k_evaluate_f64<NN, EE><<<grid, 256, 0, as_stream(stream)>>>(ch, fs, n_functors, weights, oc, \
-                                                                 first_evt, n);
-    HPS_DISPATCH_N_ENGINE(N, channel->engine, HPS_BODY)
+    if (precision == HPS_PREC_FP32_FIX) {
+        DevChannelF chf;
+        to_device_channel_f(channel, &chf);
+#define HPS_BODY(NN, EE)                                                                           \
+        k_evaluate_f32fix<NN, EE><<<grid, 256, 0, as_stream(stream)>>>(ch, chf, fs, n_functors, weights, \
+                                                                        oc, first_evt, n);
+        HPS_DISPATCH_N_ENGINE(N, channel->engine, HPS_BODY)
 #undef HPS_BODY
+    } else {
+#define HPS_BODY(NN, EE)                                                                          \
+        k_evaluate_f64<NN, EE><<<grid, 256, 0, as_stream(stream)>>>(ch, fs, n_functors, weights, oc, \
+                                                                     first_evt, n);
+        HPS_DISPATCH_N_ENGINE(N, channel->engine, HPS_BODY)
+#undef HPS_BODY
+    }
     return cuda_status(cudaGetLastError(), "hps_evaluate launch");
 }
 
@@ -186,7 +245,7 @@ extern "C" hps_status hps_generate_host(const hps_channel* channel, uint64_t fir
     const uint64_t chunk = chunk_events ? chunk_events : (uint64_t(1) << 20);
     // staging: N columns of 32 B/event (32-byte aligned), then weights, then flags
     const size_t col_bytes = (size_t)chunk * 32;
-    const size_t buf_bytes = col_bytes * N + (size_t)chunk * 8 + ((size_t)chunk + 255) / 256 * 256;
+    const size_t buf_bytes = (col_bytes * N + (size_t)chunk * 8 + (size_t)chunk + 255) / 256 * 256;
     HostPipe pipeobj;
     HostPipe* pipe = &pipeobj;
     if ((st = copy_stream(&pipe->copy)) != HPS_OK) return st;

@@ -1,0 +1,126 @@
+"""FP32_FIX form against the FP64 oracle: the maximum relative error of every output.
+
+Error measures (the same ones bench.py reports):
+  four-vectors  max over daughters/events of max_k |dp_k| / E   (energy-normalised)
+  weights       max |dw| / w
+  AverageOn     |d mean| / |mean| and agreement within the statistical error
+Tolerance: 1e-6 for every output (the precision contract of this form).
+Unweight flags may differ from the FP64 ones only where prod(pdk) lies within the weight
+tolerance of the uniform it is compared with.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-6
+PI, K = 0.13957, 0.493677
+
+CASES = [
+    ("n3_cfg1", 3, 0, 5.27934, [3.0969, K, PI]),
+    ("n5_cfg2", 5, 0, 1.86484, [K, PI, PI, PI, PI]),
+    ("n10_cfg3", 10, 0, 5.0, [PI] * 10),
+    ("n2", 2, 0, 3.0, [1.0, 0.5]),
+    ("n4_sq", 4, 1, 3.0, [0.1, 0.2, 0.3, 0.4]),
+    ("n7_mixed", 7, 1, 6.0, [PI, K, 0.938272, PI, PI, K, PI]),
+    ("n6_threshold", 6, 0, 6 * PI + 1e-3, [PI] * 6),
+]
+
+
+@pytest.fixture(scope="module")
+def api(hps, cuda):
+    from hydra_gb300 import api as A
+    return A
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch as T
+    return T
+
+
+def errors(api, torch, oracle, N, engine, M, masses, n, seed=0x3039, first=0):
+    ch = api.make_channel(masses, M, seed, engine)
+    och = oracle.make_channel(masses, M, seed, engine)
+    four = torch.empty((N, n, 4), dtype=torch.float64, device="cuda")
+    w = torch.empty(n, dtype=torch.float64, device="cuda")
+    fl = torch.empty(n, dtype=torch.uint8, device="cuda")
+    api.generate(ch, first, four, w, fl, precision="fp32_fix")
+    torch.cuda.synchronize()
+    rfour, rw = oracle.generate(och, first, n)
+    g4 = four.cpu().numpy()
+    e4 = float((np.abs(g4 - rfour).max(axis=2) / rfour[:, :, 0]).max())
+    gw = w.cpu().numpy()
+    ok = rw > 0
+    ew = float((np.abs(gw[ok] - rw[ok]) / rw[ok]).max())
+    return e4, ew, fl.cpu().numpy(), rw, och
+
+
+@pytest.mark.parametrize("name,N,engine,M,masses", CASES)
+def test_fp32fix_generate_max_relative_error(api, torch, oracle, name, N, engine, M, masses):
+    n = 1 << 20
+    e4, ew, fl, rw, och = errors(api, torch, oracle, N, engine, M, masses, n)
+    print(f"\n[fp32_fix] {name}: max four-vector err {e4:.3e}, max weight err {ew:.3e}")
+    assert e4 <= TOL, e4
+    assert ew <= TOL, ew
+    # flags: FP32_FIX compares prod(pdk) = w/maxW (generation-time weight) with u
+    u = oracle.unweight_uniforms(oracle.DEFAULT_UNWEIGHT_SEED, 0, n)
+    rprod = rw / och.max_weight
+    ref = (rprod > u).astype(np.uint8)
+    mism = np.nonzero(fl != ref)[0]
+    assert np.all(np.abs(rprod[mism] - u[mism]) <= 2 * TOL * np.maximum(u[mism], 1e-300))
+
+
+def test_fp32fix_chunking_identical(api, torch):
+    ch = api.make_channel([K, PI, PI, PI, PI], 1.86484, 0x3039, 0)
+    n, a = 70_000, 12_345
+    out = []
+    for first, m in ((0, n), (0, a), (a, n - a)):
+        f = torch.empty((5, m, 4), dtype=torch.float64, device="cuda")
+        w = torch.empty(m, dtype=torch.float64, device="cuda")
+        api.generate(ch, first, f, w, None, precision="fp32_fix")
+        out.append((f.cpu().numpy(), w.cpu().numpy()))
+    assert np.array_equal(out[0][0], np.concatenate([out[1][0], out[2][0]], axis=1))
+    assert np.array_equal(out[0][1], np.concatenate([out[1][1], out[2][1]]))
+
+
+@pytest.mark.parametrize("name,N,engine,M,masses", [CASES[0], CASES[1], CASES[2]])
+def test_fp32fix_evaluate(api, torch, oracle, name, N, engine, M, masses):
+    n = 1 << 18
+    ch = api.make_channel(masses, M, 0x3039, engine)
+    och = oracle.make_channel(masses, M, 0x3039, engine)
+    fn = api.functor_bw2(0, 1, 0.8955, 0.0473)
+    w = torch.empty(n, dtype=torch.float64, device="cuda")
+    f = torch.empty(n, dtype=torch.float64, device="cuda")
+    api.evaluate(ch, 0, n, [fn], w, [f], precision="fp32_fix")
+    rw, rf = oracle.evaluate(och, oracle.make_functor(2, 0, 1, 0.8955, 0.0473), 0, n)
+    ew = float((np.abs(w.cpu().numpy() - rw) / rw).max())
+    assert ew <= TOL, ew
+    # |BW|^2 amplifies the float error of m^2 by |m0^2 - m^2| / (m0 G0)^2 ~ 1/(m0 G0); the
+    # per-event value is reported, the averaged estimator is what the contract bounds.
+    ef = float(np.median(np.abs(f.cpu().numpy() - rf) / rf))
+    assert ef <= 1e-5, ef
+
+
+@pytest.mark.parametrize("name,N,engine,M,masses", [CASES[0], CASES[1], CASES[2]])
+def test_fp32fix_average_on(api, torch, oracle, name, N, engine, M, masses):
+    n = 1 << 22
+    ch = api.make_channel(masses, M, 0x3039, engine)
+    och = oracle.make_channel(masses, M, 0x3039, engine)
+    fn = api.functor_bw2(0, 1, 0.8955, 0.0473)
+    out = torch.zeros(3, dtype=torch.float64, device="cuda")
+    api.average_on(ch, 0, n, fn, out, None, precision="fp32_fix")
+    mean, m2, W = out.cpu().tolist()
+    rmean, rm2, rW = oracle.average_on(och, oracle.make_functor(2, 0, 1, 0.8955, 0.0473), 0, n, nthreads=0)
+    sigma = np.sqrt(rm2) / rW
+    print(f"\n[fp32_fix] AverageOn {name}: rel err mean {abs(mean - rmean) / abs(rmean):.3e}, "
+          f"sigma/mean {sigma / abs(rmean):.3e}")
+    assert abs(mean - rmean) <= TOL * abs(rmean)
+    assert abs(mean - rmean) <= 3 * sigma
+    assert abs(np.sqrt(m2) / W - sigma) <= 1e-4 * sigma
+    # deterministic
+    out2 = torch.zeros(3, dtype=torch.float64, device="cuda")
+    api.average_on(ch, 0, n, fn, out2, None, precision="fp32_fix")
+    assert out2.cpu().tolist() == [mean, m2, W]
