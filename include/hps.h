@@ -171,6 +171,26 @@ hps_status hps_average_on(const hps_channel* ch, uint64_t first_evt, uint64_t n,
                           const hps_functor* functor, hps_stats* out, void* workspace,
                           size_t workspace_bytes, int32_t precision, void* stream);
 
+/* AverageOn that makes no device allocation at all (no counterpart in the reference; Hydra's
+ * own reduction always takes temporary storage from its allocator).  It is meant for host
+ * programs that may not allocate device memory once they are running -- for example a
+ * framework that hands every byte of the GPU to its own pool at start-up, or a process held
+ * to a fixed memory quota on a shared GPU -- and so can give neither a workspace nor let the
+ * library call cudaMallocAsync.  Same arguments and result as hps_average_on without the
+ * workspace; the tile partials live in one fixed device array of HPS_NOALLOC_MAX_EVENTS /
+ * HPS_AVG_TILE entries (384 KiB) that every GPU loading the library keeps until the process
+ * exits.  Limits and rules:
+ *  - n above HPS_NOALLOC_MAX_EVENTS (2^26 events) is rejected with HPS_ERR_BAD_ARG;
+ *  - the first call on each device looks up the array's device address (with that device
+ *    current) and caches it; make that first call before any stream capture on the device;
+ *  - all calls share the one array, so calls that overlap on the GPU (different streams, or
+ *    different host threads, on the same device) race and must be serialised by the caller;
+ *  - nothing in the array needs clearing between calls: each call writes every entry it reads. */
+#define HPS_NOALLOC_MAX_EVENTS (16384ull * HPS_AVG_TILE)
+hps_status hps_average_on_noalloc(const hps_channel* ch, uint64_t first_evt, uint64_t n,
+                                  const hps_functor* functor, hps_stats* out, int32_t precision,
+                                  void* stream);
+
 /* PhaseSpaceWeight over stored events: replaces Events | Events.GetEventWeightFunctor()
  * (hydra/Decays.h:235-239, hydra/detail/Decays.inl:215-231).  out[n] = max_weight *
  * prod_i pdk(|R + p_i|, m_i, |R|). */
