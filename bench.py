@@ -74,26 +74,35 @@ class ClockSampler:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, device_index=0):
+    def __init__(self, device_index=0, period_ms=50):
         self.proc = None
-        self.lines = []
+        self.lines = []            # (host time, csv line)
         self.device_index = device_index
+        self.period_ms = period_ms
+        self.window = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device_index), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", str(self.period_ms)],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 3.0:     # sampler running before timing
+                time.sleep(0.01)
         except Exception:
             self.proc = None
         return self
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.time(), line.strip()))
+
+    def mark(self, t_start, t_end):
+        """Timed-region bounds (host clock); samples within one period of it count."""
+        self.window = (t_start - self.period_ms / 1e3, t_end + self.period_ms / 1e3)
 
     def __exit__(self, *exc):
         if self.proc is not None:
@@ -107,7 +116,14 @@ class ClockSampler:
     def summary(self):
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.lines:
+        lines = self.lines
+        if self.window is not None:
+            inside = [ln for ln in lines if self.window[0] <= ln[0] <= self.window[1]]
+            if not inside and lines:       # region shorter than a period: nearest sample
+                mid = 0.5 * (self.window[0] + self.window[1])
+                inside = [min(lines, key=lambda ln: abs(ln[0] - mid))]
+            lines = inside
+        for _, line in lines:
             parts = [x.strip() for x in line.split(",")]
             if len(parts) < 9:
                 continue
@@ -250,11 +266,13 @@ def run_gpu(args):
         torch.cuda.synchronize()
         t_start = torch.cuda.Event(enable_timing=True)
         t_end = torch.cuda.Event(enable_timing=True)
+        h0 = time.time()
         t_start.record(stream)
         for k in range(args.steps):
             step(evs[k])
         t_end.record(stream)
         torch.cuda.synchronize()
+        clocks.mark(h0, time.time())
         barrier(world)
     total_ms = t_start.elapsed_time(t_end)
     gen_ms = [e[0].elapsed_time(e[1]) for e in evs]
@@ -300,6 +318,10 @@ def run_gpu(args):
                 "traffic": traffic, "algorithmic_bytes_per_launch": n * BYTES_PER_EVENT,
                 "kernel_ms": statistics.mean(gen_ms)}
 
+    precision_report = None
+    if rank == 0 and not args.no_check:
+        precision_report = check_against_oracle(api, torch, ch, fn, first, four, w, fl, stats, args)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         rate, cores, sample = cpu_sample(seconds=3.0)
@@ -316,6 +338,7 @@ def run_gpu(args):
             "parts": {"generate_ms": statistics.mean(gen_ms), "average_on_ms": statistics.mean(avg_ms),
                       "generate_events_per_s": n / gen_avg_s,
                       "average_on_events_per_s": n / (statistics.mean(avg_ms) / 1e3)},
+            "max_rel_err": precision_report,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": 3 * args.steps, "clocks": csum,
         }
@@ -326,16 +349,46 @@ def run_gpu(args):
     return 0
 
 
+def check_against_oracle(api, torch, ch, fn, first, four, w, fl, stats, args, sample=1 << 18):
+    """Maximum relative error of this run's outputs against the FP64 oracle on the first `sample`
+    events of the step (four-vectors energy-normalised, weights relative, flags counted) and of
+    the AverageOn mean on the first 2^22 events."""
+    import numpy as np
+    from oracle import oracle as O
+    och = O.make_channel(MASSES, MOTHER, SEED, O.ENGINE_PHILOX)
+    m = min(sample, args.n)
+    rfour, rw = O.generate(och, first, m)
+    g4 = four[:, :m].cpu().numpy()
+    gw = w[:m].cpu().numpy()
+    e4 = float((np.abs(g4 - rfour).max(axis=2) / rfour[:, :, 0]).max())
+    ok = rw > 0
+    ew = float((np.abs(gw[ok] - rw[ok]) / rw[ok]).max()) if ok.any() else 0.0
+    u = O.unweight_uniforms(UNWEIGHT_SEED, first, m)
+    rfl = (rw / och.max_weight > u).astype(np.uint8)
+    nfl = int((fl[:m].cpu().numpy() != rfl).sum())
+    na = min(1 << 22, args.n)
+    out = torch.zeros(3, dtype=torch.float64, device=four.device)
+    api.average_on(ch, first, na, fn, out, None, args.precision)
+    mean = float(out[0].item())
+    rmean, rm2, rW = O.average_on(och, O.make_functor(2, *BW), first, na, nthreads=0)
+    return {"four_vectors": e4, "weights": ew, "flags_differing": nfl, "sample_events": m,
+            "average_on_mean": abs(mean - rmean) / abs(rmean), "average_on_sigma_rel": (rm2 ** 0.5 / rW) / abs(rmean),
+            "average_on_events": na,
+            "measure": "four-vectors max_k |dp_k|/E; weights |dw|/w; AverageOn |dmean|/mean vs the oracle "
+                       "(FP64, the reference's arithmetic)"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
-    ap.add_argument("--precision", choices=["fp64", "fp32_fix"], default="fp64")
+    ap.add_argument("--precision", choices=["fp64", "fp32_fix"], default="fp32_fix")
     ap.add_argument("--n", type=int, default=1 << 24)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-check", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -57,6 +57,29 @@ class HpsStats(ctypes.Structure):
     _fields_ = [("mean", ctypes.c_double), ("m2", ctypes.c_double), ("w", ctypes.c_double)]
 
 
+class HpsBatchItem(ctypes.Structure):
+    _fields_ = [
+        ("channel", HpsChannel),
+        ("first_evt", ctypes.c_uint64),
+        ("n_events", ctypes.c_uint64),
+        ("mode", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("functor", HpsFunctor),
+        ("cols", ctypes.c_void_p * HPS_MAX_DAUGHTERS),
+        ("weights", ctypes.c_void_p),
+        ("flags", ctypes.c_void_p),
+        ("unweight_seed", ctypes.c_uint64),
+        ("stats", ctypes.c_void_p),
+    ]
+
+
+class HpsBatchTuning(ctypes.Structure):
+    _fields_ = [("ctas_per_sm", ctypes.c_int32), ("store_tile_events", ctypes.c_int32)]
+
+
+MODE_STORE, MODE_AVERAGE = 0, 1
+
+
 class HpsError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"hps status {status}: {message}")
@@ -80,6 +103,13 @@ SIGNATURES = {
     "hps_unweight_flags": (_i32, [_i32, _vp, _dbl, _u64, _vp, _u64, _u64, _vp, _vp]),
     "hps_rng_words": (_i32, [_i32, _i32, _u64, _u64, _u64, _vp, _vp]),
     "hps_default_seed": (_u64, [_i32, _vp]),
+    "hps_batch_create": (_i32, [_vp, _i32, _u64, _i32, _vp]),
+    "hps_batch_set_items": (_i32, [_vp, _vp, _i32, _vp]),
+    "hps_batch_launch": (_i32, [_vp, _vp]),
+    "hps_batch_get_tuning": (_i32, [_vp, _vp]),
+    "hps_batch_set_tuning": (_i32, [_vp, _vp]),
+    "hps_batch_autotune": (_i32, [_vp, _vp, ctypes.c_char_p, _vp]),
+    "hps_batch_destroy": (_i32, [_vp]),
     "hps_last_error": (ctypes.c_char_p, []),
     "hps_abi_version": (_i32, []),
 }

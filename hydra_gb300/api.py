@@ -20,6 +20,7 @@ from typing import Iterable, Sequence
 import torch
 
 from . import (
+    MODE_AVERAGE, MODE_STORE, HpsBatchItem, HpsBatchTuning,
     DEFAULT_UNWEIGHT_SEED, ENGINE_PHILOX, ENGINE_SQUARES3, ERR_BAD_ARG, ERR_NO_ENERGY, FN_BW2, FN_MASS2, FN_ONE,
     HPS_MAX_DAUGHTERS, PREC_FP32_FIX, PREC_FP64, HpsChannel, HpsError, HpsFunctor, check, lib,
 )
@@ -193,6 +194,80 @@ def rng_words(n_daughters: int, engine, seed: int, first: int, n: int, out: torc
         raise ValueError("out must be 64-bit with n*(3N-4) elements")
     check(lib().hps_rng_words(n_daughters, _ENGINES[engine], int(seed) & (2**64 - 1), first, n, _dptr(out),
                               _stream_handle(stream)))
+
+
+# ----------------------------------------------------------------------------- batched channels
+
+def store_item(ch: HpsChannel, first: int, four: torch.Tensor, weights=None, flags=None,
+               unweight_seed: int = DEFAULT_UNWEIGHT_SEED) -> HpsBatchItem:
+    it = HpsBatchItem()
+    it.channel = ch
+    it.first_evt = first
+    it.n_events = four.shape[1]
+    it.mode = MODE_STORE
+    for k in range(ch.n_daughters):
+        it.cols[k] = four[k].data_ptr()
+    it.weights = weights.data_ptr() if weights is not None else None
+    it.flags = flags.data_ptr() if flags is not None else None
+    it.unweight_seed = unweight_seed & (2**64 - 1)
+    return it
+
+
+def average_item(ch: HpsChannel, first: int, n: int, functor: HpsFunctor, stats: torch.Tensor) -> HpsBatchItem:
+    it = HpsBatchItem()
+    it.channel = ch
+    it.first_evt = first
+    it.n_events = n
+    it.mode = MODE_AVERAGE
+    it.functor = functor
+    it.stats = stats.data_ptr()
+    return it
+
+
+class BatchPlan:
+    """Many channels in one persistent, graph-captured launch (hps_batch_*; FP32_FIX)."""
+
+    def __init__(self, max_items: int, max_average_tiles: int, tuning: tuple[int, int] | None = None):
+        self._p = ctypes.c_void_p()
+        t = HpsBatchTuning(*tuning) if tuning else None
+        check(lib().hps_batch_create(ctypes.byref(self._p), max_items, max_average_tiles, PREC_FP32_FIX,
+                                     ctypes.byref(t) if t else None))
+        self._items = None
+
+    def set_items(self, items: Sequence[HpsBatchItem], stream=None):
+        arr = (HpsBatchItem * max(1, len(items)))(*items)
+        self._items = arr
+        check(lib().hps_batch_set_items(self._p, ctypes.cast(arr, ctypes.c_void_p), len(items),
+                                        _stream_handle(stream)))
+
+    def launch(self, stream=None):
+        check(lib().hps_batch_launch(self._p, _stream_handle(stream)))
+
+    def tuning(self) -> tuple[int, int]:
+        t = HpsBatchTuning()
+        check(lib().hps_batch_get_tuning(self._p, ctypes.byref(t)))
+        return t.ctas_per_sm, t.store_tile_events
+
+    def set_tuning(self, ctas_per_sm: int, store_tile_events: int):
+        t = HpsBatchTuning(ctas_per_sm, store_tile_events)
+        check(lib().hps_batch_set_tuning(self._p, ctypes.byref(t)))
+
+    def autotune(self, cache_path: str | None = None, stream=None) -> tuple[int, int]:
+        t = HpsBatchTuning()
+        check(lib().hps_batch_autotune(self._p, _stream_handle(stream),
+                                       cache_path.encode() if cache_path else None, ctypes.byref(t)))
+        return t.ctas_per_sm, t.store_tile_events
+
+    def close(self):
+        if self._p:
+            lib().hps_batch_destroy(self._p)
+            self._p = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ----------------------------------------------------------------------------- reference-shaped API

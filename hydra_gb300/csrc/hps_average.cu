@@ -11,13 +11,11 @@
 // Which CTA runs which tile does not matter, so the result is bit-identical for every grid.
 #include "common.h"
 #include "store.cuh"
+#include "tiles_f32.cuh"
 
 namespace hps {
 
-constexpr int kAvgThreads = 256;
-constexpr int kAvgPerThread = HPS_AVG_TILE / kAvgThreads;
-static_assert(kAvgThreads * kAvgPerThread == HPS_AVG_TILE, "tile shape");
-constexpr int kFinalThreads = 1024;
+constexpr int kAvgThreads = kTileThreads;
 
 template <int N, int ENGINE>
 __global__ void __launch_bounds__(kAvgThreads)
@@ -43,42 +41,15 @@ k_average_tiles_f64(DevChannel ch, DevFunctor fn, uint64_t first, uint64_t n, ui
     }
 }
 
-// FP32_FIX form: the event (kinematics in float) and the functor value in float; each thread
-// accumulates its events as shifted weighted sums in double (W, sum w(f-K), sum w(f-K)^2 with K
-// its first value), which is the StatsPHSP of those events in closed form, then the same fixed
-// warp/CTA tree merges the per-thread StatsPHSP.
+// FP32_FIX form: average_tile_f32 (tiles_f32.cuh) per tile, CTA-shared random words.
 template <int N, int ENGINE>
 __global__ void __launch_bounds__(kAvgThreads)
 k_average_tiles_f32fix(DevChannel chd, DevChannelF ch, DevFunctor fn, uint64_t first, uint64_t n,
                        uint64_t ntiles, hps_stats* __restrict__ partials)
 {
+    __shared__ __align__(16) unsigned char smem[WordShare<N, ENGINE, kAvgThreads>::BYTES];
     for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        double sw = 0.0, s1 = 0.0, s2 = 0.0;
-        float K = 0.0f;
-        const uint64_t base = t * HPS_AVG_TILE + threadIdx.x;
-        for (int k = 0; k < kAvgPerThread; ++k) {
-            const uint64_t e = base + (uint64_t)k * kAvgThreads;
-            if (e < n) {
-                float p[N][4];
-                double prod;
-                const double w = f32::event<N, ENGINE>(chd, ch, first + e, p, prod);
-                const float f = f32::functor<N>(fn, p);
-                if (k == 0) K = f;
-                const double d = f32::widen(f - K);
-                const double wd = w * d;
-                sw += w;
-                s1 += wd;
-                s2 = fma(wd, d, s2);
-            }
-        }
-        hps_stats acc{0.0, 0.0, 0.0};
-        if (sw != 0.0) {
-            const double q = s1 / sw;
-            acc.w = sw;
-            acc.mean = f32::widen(K) + q;
-            acc.m2 = fma(-s1, q, s2);
-        }
-        const hps_stats r = block_reduce_stats<kAvgThreads>(acc);
+        const hps_stats r = average_tile_f32<N, ENGINE>(chd, ch, fn, first, n, t, smem);
         if (threadIdx.x == 0) partials[t] = r;
     }
 }
@@ -87,9 +58,7 @@ k_average_tiles_f32fix(DevChannel chd, DevChannelF ch, DevFunctor fn, uint64_t f
 __global__ void __launch_bounds__(kFinalThreads)
 k_average_final(const hps_stats* __restrict__ partials, uint64_t ntiles, hps_stats* __restrict__ out)
 {
-    hps_stats acc{0.0, 0.0, 0.0};
-    for (uint64_t t = threadIdx.x; t < ntiles; t += kFinalThreads) acc = stats_merge(acc, partials[t]);
-    const hps_stats r = block_reduce_stats<kFinalThreads>(acc);
+    const hps_stats r = merge_partials(partials, ntiles);
     if (threadIdx.x == 0) *out = r;
 }
 

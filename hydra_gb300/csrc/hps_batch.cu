@@ -1,0 +1,462 @@
+// hps_batch.cu -- many channels of different N in one persistent, graph-captured launch.
+//
+// The items of a plan are cut into work units: a store item into units of store_tile events,
+// an AverageOn item into tiles of HPS_AVG_TILE events.  A persistent grid of 256-thread CTAs
+// takes units from a device counter; each unit dispatches on (N, engine, mode) to the same
+// work-unit functions the single-channel FP32_FIX kernels use (tiles_f32.cuh), so an item's
+// outputs do not depend on what else is in the batch.  A second kernel merges each AverageOn
+// item's tile partials with the fixed tree of hps_average_on.  Counter reset, persistent kernel
+// and merge are captured once into a CUDA graph; the item table and its header live in device
+// memory, so new items need no re-capture.
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+#include <fstream>
+#include <sstream>
+
+#include "common.h"
+#include "store.cuh"
+#include "tiles_f32.cuh"
+
+namespace hps {
+
+struct BatchItemDev {
+    DevChannel chd;
+    DevChannelF chf;
+    DevFunctor fn;
+    Cols cols;
+    double* weights;
+    uint8_t* flags;
+    hps_stats* stats;
+    uint64_t first, n, ukey;
+    uint64_t unit_begin;       // first global work unit of this item
+    uint64_t partial_offset;   // AverageOn: offset of its tile partials
+    uint64_t units;            // work units of this item
+    int32_t mode, N, engine, vec32;
+};
+
+struct BatchHeader {
+    unsigned long long counter;   // next work unit (reset by the graph before each launch)
+    uint64_t total_units;
+    int32_t n_items;
+    int32_t store_tile;
+};
+
+// Largest shared-memory word exchange over N and engines (Philox, N = 10).
+constexpr int kBatchSmem = WordShare<10, kPhilox, kTileThreads>::BYTES;
+
+template <int N, int ENGINE>
+__device__ __forceinline__ void run_unit(const BatchItemDev& it, uint64_t u, int store_tile, hps_stats* partials,
+                                         void* smem)
+{
+    if (it.mode == HPS_MODE_STORE) {
+        const uint64_t lo = u * (uint64_t)store_tile;
+        const uint64_t hi = (lo + store_tile < it.n) ? lo + store_tile : it.n;
+        for (uint64_t cb = lo; cb < hi; cb += kTileThreads)
+            store_chunk_f32<N, ENGINE>(it.chd, it.chf, it.cols, it.weights, it.flags, it.ukey, it.first, hi, cb,
+                                       it.vec32 != 0, smem);
+    } else {
+        const hps_stats r = average_tile_f32<N, ENGINE>(it.chd, it.chf, it.fn, it.first, it.n, u, smem);
+        if (threadIdx.x == 0) partials[it.partial_offset + u] = r;
+    }
+}
+
+__global__ void __launch_bounds__(kTileThreads)
+k_batch_f32(const BatchItemDev* __restrict__ items, BatchHeader* __restrict__ hdr, hps_stats* __restrict__ partials)
+{
+    __shared__ __align__(16) unsigned char smem[kBatchSmem];
+    __shared__ unsigned long long s_unit;
+    __shared__ int s_item;
+    const uint64_t total = hdr->total_units;
+    const int n_items = hdr->n_items;
+    const int store_tile = hdr->store_tile;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const unsigned long long u = atomicAdd(&hdr->counter, 1ull);
+            int lo = 0, hi = n_items - 1;                 // last item with unit_begin <= u
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (items[mid].unit_begin <= u) lo = mid; else hi = mid - 1;
+            }
+            s_unit = u;
+            s_item = lo;
+        }
+        __syncthreads();
+        const unsigned long long u = s_unit;
+        const BatchItemDev& it = items[s_item];
+        __syncthreads();                                  // s_unit / s_item read before they change
+        if (u >= total) return;
+        const uint64_t lu = u - it.unit_begin;
+        switch (it.N * 2 + it.engine) {
+#define HPS_UNIT(NN)                                                                         \
+        case NN * 2 + 0: run_unit<NN, kPhilox>(it, lu, store_tile, partials, smem); break;   \
+        case NN * 2 + 1: run_unit<NN, kSquares3>(it, lu, store_tile, partials, smem); break;
+        HPS_UNIT(2) HPS_UNIT(3) HPS_UNIT(4) HPS_UNIT(5) HPS_UNIT(6) HPS_UNIT(7) HPS_UNIT(8) HPS_UNIT(9)
+        HPS_UNIT(10)
+#undef HPS_UNIT
+        default: break;
+        }
+    }
+}
+
+// One CTA per item slot: AverageOn items merge their tile partials exactly as hps_average_on.
+__global__ void __launch_bounds__(kFinalThreads)
+k_batch_merge(const BatchItemDev* __restrict__ items, const BatchHeader* __restrict__ hdr,
+              const hps_stats* __restrict__ partials)
+{
+    if ((int)blockIdx.x >= hdr->n_items) return;
+    const BatchItemDev& it = items[blockIdx.x];
+    if (it.mode != HPS_MODE_AVERAGE) return;
+    const hps_stats r = merge_partials(partials + it.partial_offset, it.units);
+    if (threadIdx.x == 0) *it.stats = r;
+}
+
+}  // namespace hps
+
+using namespace hps;
+
+struct hps_batch_plan {
+    int device = 0;
+    int sm_count = 0;
+    int32_t max_items = 0;
+    uint64_t max_avg_tiles = 0;
+    int32_t precision = HPS_PREC_FP32_FIX;
+    hps_batch_tuning tuning{2, 16384};
+    BatchItemDev* d_items = nullptr;
+    BatchHeader* d_header = nullptr;
+    hps_stats* d_partials = nullptr;
+    BatchItemDev* h_items = nullptr;   // pinned staging
+    BatchHeader* h_header = nullptr;   // pinned staging
+    cudaEvent_t staged = nullptr;      // staging copy finished
+    bool staged_pending = false;
+    int32_t n_items = 0;
+    std::vector<hps_batch_item> items;  // host copy, re-cut when the store tile changes
+    uint64_t total_events = 0;
+    std::vector<int> mix;              // item mix signature for the tuning cache
+    cudaStream_t capture = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+hps_status destroy_graph(hps_batch_plan* p)
+{
+    if (p->exec) {
+        cudaError_t e = cudaGraphExecDestroy(p->exec);
+        p->exec = nullptr;
+        if (e != cudaSuccess) return cuda_status(e, "cudaGraphExecDestroy");
+    }
+    return HPS_OK;
+}
+
+hps_status build_graph(hps_batch_plan* p)
+{
+    hps_status st = destroy_graph(p);
+    if (st != HPS_OK) return st;
+    const unsigned grid = static_cast<unsigned>(p->tuning.ctas_per_sm * p->sm_count);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(p->capture, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_status(e, "cudaStreamBeginCapture");
+    cudaMemsetAsync(&p->d_header->counter, 0, sizeof(unsigned long long), p->capture);
+    k_batch_f32<<<grid, kTileThreads, 0, p->capture>>>(p->d_items, p->d_header, p->d_partials);
+    k_batch_merge<<<static_cast<unsigned>(p->max_items), kFinalThreads, 0, p->capture>>>(p->d_items, p->d_header,
+                                                                                         p->d_partials);
+    e = cudaStreamEndCapture(p->capture, &graph);
+    if (e != cudaSuccess) return cuda_status(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&p->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        p->exec = nullptr;
+        return cuda_status(e, "cudaGraphInstantiate");
+    }
+    return HPS_OK;
+}
+
+hps_status check_tuning(const hps_batch_tuning* t)
+{
+    if (t->ctas_per_sm < 1 || t->ctas_per_sm > 16)
+        return set_error(HPS_ERR_BAD_ARG, "ctas_per_sm %d outside 1..16", t->ctas_per_sm);
+    if (t->store_tile_events < kTileThreads || t->store_tile_events % kTileThreads != 0 ||
+        t->store_tile_events > (1 << 24))
+        return set_error(HPS_ERR_BAD_ARG, "store_tile_events %d not a multiple of 256 in 256..2^24",
+                         t->store_tile_events);
+    return HPS_OK;
+}
+
+std::string tuning_key(const hps_batch_plan* p)
+{
+    cudaDeviceProp prop;
+    std::ostringstream os;
+    if (cudaGetDeviceProperties(&prop, p->device) == cudaSuccess) {
+        std::string name(prop.name);
+        for (char& c : name) if (c == ' ') c = '_';
+        os << name;
+    } else {
+        os << "gpu";
+    }
+    os << "|p" << p->precision << "|";
+    for (int v : p->mix) os << v << ",";
+    return os.str();
+}
+
+hps_status item_error(hps_status st, int i)
+{
+    char msg[400];
+    std::snprintf(msg, sizeof(msg), "%s", hps_last_error());
+    return set_error(st, "item %d: %s", i, msg);
+}
+
+// Validates items, cuts them into work units with the plan's store tile, fills the pinned
+// staging table and uploads it on `s`.
+hps_status upload_items(hps_batch_plan* p, const std::vector<hps_batch_item>& items, cudaStream_t s)
+{
+    // the staging copy of the previous upload must have left the pinned buffer
+    if (p->staged_pending) {
+        cudaError_t e = cudaEventSynchronize(p->staged);
+        if (e != cudaSuccess) return cuda_status(e, "cudaEventSynchronize");
+        p->staged_pending = false;
+    }
+    const int n_items = static_cast<int>(items.size());
+    uint64_t unit = 0, partial = 0, events = 0;
+    std::vector<int> mix(2 * 11 * 2, 0);
+    for (int i = 0; i < n_items; ++i) {
+        const hps_batch_item& in = items[i];
+        BatchItemDev& d = p->h_items[i];
+        std::memset(&d, 0, sizeof(d));
+        hps_status st = to_device_channel(&in.channel, &d.chd);
+        if (st != HPS_OK) return item_error(st, i);
+        to_device_channel_f(&in.channel, &d.chf);
+        if (!range_ok(in.first_evt, in.n_events)) return set_error(HPS_ERR_BAD_ARG, "item %d: event range wraps", i);
+        const int N = in.channel.n_daughters;
+        d.N = N;
+        d.engine = in.channel.engine;
+        d.mode = in.mode;
+        d.first = in.first_evt;
+        d.n = in.n_events;
+        d.unit_begin = unit;
+        if (in.mode == HPS_MODE_STORE) {
+            bool all32 = true;
+            for (int k = 0; k < N; ++k) {
+                if (in.n_events && !in.cols[k]) return set_error(HPS_ERR_BAD_ARG, "item %d: column %d is NULL", i, k);
+                if (!aligned(in.cols[k], 16)) return set_error(HPS_ERR_BAD_ARG, "item %d: column %d misaligned", i, k);
+                all32 = all32 && aligned(in.cols[k], 32);
+                d.cols.p[k] = in.cols[k];
+            }
+            if (in.weights && !aligned(in.weights, 8)) return set_error(HPS_ERR_BAD_ARG, "item %d: weights misaligned", i);
+            d.vec32 = all32 ? 1 : 0;
+            d.weights = in.weights;
+            d.flags = in.flags;
+            d.ukey = splitmix64(in.unweight_seed);
+            d.units = (in.n_events + p->tuning.store_tile_events - 1) / p->tuning.store_tile_events;
+        } else if (in.mode == HPS_MODE_AVERAGE) {
+            st = to_device_functor(&in.functor, N, &d.fn);
+            if (st != HPS_OK) return item_error(st, i);
+            if (!in.stats || !aligned(in.stats, 8)) return set_error(HPS_ERR_BAD_ARG, "item %d: stats missing", i);
+            d.stats = in.stats;
+            d.units = (in.n_events + HPS_AVG_TILE - 1) / HPS_AVG_TILE;
+            d.partial_offset = partial;
+            partial += d.units;
+            if (partial > p->max_avg_tiles)
+                return set_error(HPS_ERR_BUDGET, "AverageOn tiles %llu exceed the plan's %llu",
+                                 (unsigned long long)partial, (unsigned long long)p->max_avg_tiles);
+        } else {
+            return set_error(HPS_ERR_BAD_ARG, "item %d: unknown mode %d", i, in.mode);
+        }
+        unit += d.units;
+        events += in.n_events;
+        mix[(in.mode * 11 + N) * 2 + d.engine] += 1;
+    }
+    p->h_header->counter = 0;
+    p->h_header->total_units = unit;
+    p->h_header->n_items = n_items;
+    p->h_header->store_tile = p->tuning.store_tile_events;
+    p->n_items = n_items;
+    p->total_events = events;
+    p->mix = mix;
+    p->mix.push_back(events ? 63 - __builtin_clzll(events) : 0);   // log2 of the event count
+    cudaError_t e = cudaSuccess;
+    if (n_items) e = cudaMemcpyAsync(p->d_items, p->h_items, sizeof(BatchItemDev) * n_items, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_header, p->h_header, sizeof(BatchHeader), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaEventRecord(p->staged, s);
+    if (e != cudaSuccess) return cuda_status(e, "batch table upload");
+    p->staged_pending = true;
+    return HPS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+hps_status hps_batch_create(hps_batch_plan** out, int32_t max_items, uint64_t max_average_tiles, int32_t precision,
+                            const hps_batch_tuning* tuning)
+{
+    clear_error();
+    if (!out) return set_error(HPS_ERR_BAD_ARG, "plan is NULL");
+    *out = nullptr;
+    if (max_items < 1 || max_items > (1 << 20)) return set_error(HPS_ERR_BAD_ARG, "max_items %d", max_items);
+    if (precision != HPS_PREC_FP32_FIX)
+        return set_error(HPS_ERR_UNSUPPORTED, "the batched kernel is built for HPS_PREC_FP32_FIX only");
+    if (tuning) {
+        hps_status st = check_tuning(tuning);
+        if (st != HPS_OK) return st;
+    }
+    hps_batch_plan* p = new hps_batch_plan();
+    p->max_items = max_items;
+    p->max_avg_tiles = max_average_tiles ? max_average_tiles : 1;
+    p->precision = precision;
+    if (tuning) p->tuning = *tuning;
+    cudaError_t e = cudaGetDevice(&p->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&p->sm_count, cudaDevAttrMultiProcessorCount, p->device);
+    if (e == cudaSuccess) e = cudaMalloc(&p->d_items, sizeof(BatchItemDev) * max_items);
+    if (e == cudaSuccess) e = cudaMalloc(&p->d_header, sizeof(BatchHeader));
+    if (e == cudaSuccess) e = cudaMalloc(&p->d_partials, sizeof(hps_stats) * p->max_avg_tiles);
+    if (e == cudaSuccess) e = cudaMallocHost(&p->h_items, sizeof(BatchItemDev) * max_items);
+    if (e == cudaSuccess) e = cudaMallocHost(&p->h_header, sizeof(BatchHeader));
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->staged, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->capture, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMemset(p->d_header, 0, sizeof(BatchHeader));
+    if (e != cudaSuccess) {
+        hps_status st = (e == cudaErrorMemoryAllocation) ? set_error(HPS_ERR_OOM, "batch plan: %s", cudaGetErrorString(e))
+                                                         : cuda_status(e, "batch plan");
+        hps_batch_destroy(p);
+        return st;
+    }
+    std::memset(p->h_header, 0, sizeof(BatchHeader));
+    hps_status st = build_graph(p);
+    if (st != HPS_OK) {
+        hps_batch_destroy(p);
+        return st;
+    }
+    *out = p;
+    return HPS_OK;
+}
+
+hps_status hps_batch_set_items(hps_batch_plan* p, const hps_batch_item* items, int32_t n_items, void* stream)
+{
+    clear_error();
+    if (!p) return set_error(HPS_ERR_BAD_ARG, "plan is NULL");
+    if (n_items < 0 || n_items > p->max_items)
+        return set_error(HPS_ERR_BAD_ARG, "n_items %d outside 0..%d", n_items, p->max_items);
+    if (n_items > 0 && !items) return set_error(HPS_ERR_BAD_ARG, "items is NULL");
+    std::vector<hps_batch_item> copy(items, items + n_items);
+    hps_status st = upload_items(p, copy, as_stream(stream));
+    if (st == HPS_OK) p->items.swap(copy);
+    return st;
+}
+
+hps_status hps_batch_launch(hps_batch_plan* p, void* stream)
+{
+    clear_error();
+    if (!p) return set_error(HPS_ERR_BAD_ARG, "plan is NULL");
+    if (!p->exec) {
+        hps_status st = build_graph(p);
+        if (st != HPS_OK) return st;
+    }
+    return cuda_status(cudaGraphLaunch(p->exec, as_stream(stream)), "cudaGraphLaunch");
+}
+
+hps_status hps_batch_get_tuning(const hps_batch_plan* p, hps_batch_tuning* out)
+{
+    clear_error();
+    if (!p || !out) return set_error(HPS_ERR_BAD_ARG, "NULL argument");
+    *out = p->tuning;
+    return HPS_OK;
+}
+
+hps_status hps_batch_set_tuning(hps_batch_plan* p, const hps_batch_tuning* t)
+{
+    clear_error();
+    if (!p || !t) return set_error(HPS_ERR_BAD_ARG, "NULL argument");
+    hps_status st = check_tuning(t);
+    if (st != HPS_OK) return st;
+    const bool tile_changed = t->store_tile_events != p->tuning.store_tile_events;
+    p->tuning = *t;
+    if (tile_changed && p->n_items > 0) {
+        // re-cut the current items into the new store tile; done on the plan's own stream
+        st = upload_items(p, p->items, p->capture);
+        if (st != HPS_OK) return st;
+        cudaError_t e = cudaStreamSynchronize(p->capture);
+        if (e != cudaSuccess) return cuda_status(e, "cudaStreamSynchronize");
+    }
+    return build_graph(p);
+}
+
+hps_status hps_batch_autotune(hps_batch_plan* p, void* stream, const char* cache_path, hps_batch_tuning* chosen)
+{
+    clear_error();
+    if (!p) return set_error(HPS_ERR_BAD_ARG, "plan is NULL");
+    if (p->n_items == 0) return set_error(HPS_ERR_BAD_ARG, "no items to tune on");
+    static std::mutex cache_mu;
+    const std::string key = tuning_key(p);
+    if (cache_path) {
+        std::lock_guard<std::mutex> lock(cache_mu);
+        std::ifstream in(cache_path);
+        std::string line;
+        while (std::getline(in, line)) {
+            std::istringstream ls(line);
+            std::string k;
+            hps_batch_tuning t;
+            double ms;
+            if ((ls >> k >> t.ctas_per_sm >> t.store_tile_events >> ms) && k == key && check_tuning(&t) == HPS_OK) {
+                hps_status st = hps_batch_set_tuning(p, &t);
+                if (st == HPS_OK && chosen) *chosen = t;
+                return st;
+            }
+        }
+    }
+    cudaStream_t s = as_stream(stream);
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    const int ctas[] = {1, 2, 3, 4, 6, 8};
+    const int tiles[] = {4096, 16384, 65536};
+    std::vector<hps_batch_tuning> cands;
+    for (int tile : tiles)
+        for (int c : ctas) cands.push_back(hps_batch_tuning{c, tile});
+    hps_batch_tuning best = p->tuning;
+    float best_ms = 1e30f;
+    hps_status st = HPS_OK;
+    for (const hps_batch_tuning& t : cands) {
+        if ((st = hps_batch_set_tuning(p, &t)) != HPS_OK) break;
+        if ((st = hps_batch_launch(p, stream)) != HPS_OK) break;       // warm-up
+        cudaEventRecord(a, s);
+        for (int r = 0; r < 3 && st == HPS_OK; ++r) st = hps_batch_launch(p, stream);
+        cudaEventRecord(b, s);
+        cudaError_t e = cudaEventSynchronize(b);
+        if (e != cudaSuccess) { st = cuda_status(e, "autotune timing"); break; }
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, a, b);
+        if (ms < best_ms) { best_ms = ms; best = t; }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (st != HPS_OK) return st;
+    st = hps_batch_set_tuning(p, &best);
+    if (st != HPS_OK) return st;
+    if (cache_path) {
+        std::lock_guard<std::mutex> lock(cache_mu);
+        std::ofstream outf(cache_path, std::ios::app);
+        outf << key << " " << best.ctas_per_sm << " " << best.store_tile_events << " " << best_ms / 3.0f << "\n";
+    }
+    if (chosen) *chosen = best;
+    return HPS_OK;
+}
+
+hps_status hps_batch_destroy(hps_batch_plan* p)
+{
+    if (!p) return HPS_OK;
+    destroy_graph(p);
+    if (p->staged) { cudaEventSynchronize(p->staged); cudaEventDestroy(p->staged); }
+    if (p->capture) cudaStreamDestroy(p->capture);
+    if (p->d_items) cudaFree(p->d_items);
+    if (p->d_header) cudaFree(p->d_header);
+    if (p->d_partials) cudaFree(p->d_partials);
+    if (p->h_items) cudaFreeHost(p->h_items);
+    if (p->h_header) cudaFreeHost(p->h_header);
+    delete p;
+    return HPS_OK;
+}
+
+}  // extern "C"

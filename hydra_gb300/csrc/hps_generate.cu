@@ -9,10 +9,9 @@
 
 #include "common.h"
 #include "store.cuh"
+#include "tiles_f32.cuh"
 
 namespace hps {
-
-struct Cols { double* p[HPS_MAX_DAUGHTERS]; };
 
 template <int N, int ENGINE>
 __global__ void __launch_bounds__(256)
@@ -35,32 +34,22 @@ k_generate_f64(DevChannel ch, Cols cols, double* __restrict__ weights, uint8_t* 
     }
 }
 
-// FP32_FIX store path: kinematics in float (light-cone boosts, exact-octant angles),
-// weight and unweight test in double; four-vectors widened to double for the Decays columns.
-// The unweight flag compares prod(pdk) -- weight / max_weight, the quantity FlagDaugthers
-// tests -- with u, using the generation-time weight.
+// FP32_FIX store path: kinematics in float (light-cone boosts, exact-octant angles), weight
+// finished in double, four-vectors widened to double for the Decays columns.  Each CTA takes 256
+// consecutive events per CTA iteration and shares their random words (cta_event_words).  The unweight flag tests
+// prod(pdk) -- weight / max_weight, the quantity FlagDaugthers tests -- against u using the
+// generation-time weight.
+constexpr int kGenThreads = kTileThreads;
+
 template <int N, int ENGINE>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kGenThreads)
 k_generate_f32fix(DevChannel chd, DevChannelF ch, Cols cols, double* __restrict__ weights,
                   uint8_t* __restrict__ flags, uint64_t ukey, uint64_t first, uint64_t n, int vec32)
 {
-    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < n;
-         e += (uint64_t)gridDim.x * blockDim.x) {
-        float p[N][4];
-        double prod;
-        const double wt = f32::event<N, ENGINE>(chd, ch, first + e, p, prod);
-#pragma unroll
-        for (int k = 0; k < N; ++k) {
-            const double v[4] = {f32::widen(p[k][0]), f32::widen(p[k][1]), f32::widen(p[k][2]),
-                                 f32::widen(p[k][3])};
-            store_vec4(cols.p[k], e, v, vec32 != 0);
-        }
-        if (weights) weights[e] = wt;
-        if (flags) {
-            const double u = static_cast<double>(squares3_word(ukey, first + e)) * 0x1p-32;
-            flags[e] = (prod > u) ? 1 : 0;
-        }
-    }
+    __shared__ __align__(16) unsigned char smem[WordShare<N, ENGINE, kGenThreads>::BYTES];
+    const uint64_t step = (uint64_t)gridDim.x * kGenThreads;
+    for (uint64_t cb = (uint64_t)blockIdx.x * kGenThreads; cb < n; cb += step)
+        store_chunk_f32<N, ENGINE>(chd, ch, cols, weights, flags, ukey, first, n, cb, vec32 != 0, smem);
 }
 
 constexpr int kMaxFunctors = 8;
@@ -82,17 +71,22 @@ k_evaluate_f64(DevChannel ch, Functors fs, int nf, double* __restrict__ weights,
 }
 
 template <int N, int ENGINE>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kGenThreads)
 k_evaluate_f32fix(DevChannel chd, DevChannelF ch, Functors fs, int nf, double* __restrict__ weights,
                   OutCols out, uint64_t first, uint64_t n)
 {
-    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < n;
-         e += (uint64_t)gridDim.x * blockDim.x) {
-        float p[N][4];
-        double prod;
-        const double wt = f32::event<N, ENGINE>(chd, ch, first + e, p, prod);
-        if (weights) weights[e] = wt;
-        for (int k = 0; k < nf; ++k) out.p[k][e] = f32::widen(f32::functor<N>(fs.f[k], p));
+    __shared__ __align__(16) unsigned char smem[WordShare<N, ENGINE, kGenThreads>::BYTES];
+    const uint64_t step = (uint64_t)gridDim.x * kGenThreads;
+    for (uint64_t cb = (uint64_t)blockIdx.x * kGenThreads; cb < n; cb += step) {
+        uint64_t w[3 * N - 4];
+        cta_event_words<N, ENGINE, kGenThreads>(chd.key, first + cb, smem, w);
+        const uint64_t e = cb + threadIdx.x;
+        if (e < n) {
+            float p[N][4];
+            const f32::EventWeight ew = f32::event_from_words<N, ENGINE>(chd, ch, w, p);
+            if (weights) weights[e] = ew.weight;
+            for (int k = 0; k < nf; ++k) out.p[k][e] = f32::widen(f32::functor<N>(fs.f[k], p));
+        }
     }
 }
 
@@ -132,7 +126,7 @@ hps_status hps_generate(const hps_channel* channel, uint64_t first_evt, uint64_t
         DevChannelF chf;
         to_device_channel_f(channel, &chf);
 #define HPS_BODY(NN, EE)                                                                         \
-        k_generate_f32fix<NN, EE><<<grid, 256, 0, as_stream(stream)>>>(ch, chf, cc, weights, flags, ukey, \
+        k_generate_f32fix<NN, EE><<<grid, kGenThreads, 0, as_stream(stream)>>>(ch, chf, cc, weights, flags, ukey, \
                                                                         first_evt, n, vec32);
         HPS_DISPATCH_N_ENGINE(N, channel->engine, HPS_BODY)
 #undef HPS_BODY
@@ -173,7 +167,7 @@ hps_status hps_evaluate(const hps_channel* channel, uint64_t first_evt, uint64_t
         DevChannelF chf;
         to_device_channel_f(channel, &chf);
 #define HPS_BODY(NN, EE)                                                                           \
-        k_evaluate_f32fix<NN, EE><<<grid, 256, 0, as_stream(stream)>>>(ch, chf, fs, n_functors, weights, \
+        k_evaluate_f32fix<NN, EE><<<grid, kGenThreads, 0, as_stream(stream)>>>(ch, chf, fs, n_functors, weights, \
                                                                         oc, first_evt, n);
         HPS_DISPATCH_N_ENGINE(N, channel->engine, HPS_BODY)
 #undef HPS_BODY

@@ -111,3 +111,67 @@ __device__ __forceinline__ void sort_words(uint64_t* w)
 }
 
 }  // namespace hps
+
+namespace hps {
+
+// ---------------------------------------------------------------------------------------------
+// CTA-shared random words.  Event e draws the stream at counters e+3N+1+b (Philox blocks) or
+// e+3N+k (squares3 words), so the NT consecutive events of a CTA need only NT + B - 1 distinct
+// Philox blocks (B = blocks per event) instead of NT*B: each thread computes one block (B - 1
+// threads a second), parks it in shared memory, and reads back the B blocks of its own event.
+// The words are the same words, bit for bit; only who computes them changes.
+// ---------------------------------------------------------------------------------------------
+
+template <int N, int ENGINE, int NT> struct WordShare {
+    static constexpr int NW = 3 * N - 4;
+    static constexpr int B = (ENGINE == kPhilox) ? (NW + 1) / 2 : NW;   // items per event
+    static constexpr int SLOTS = NT + B - 1;
+    static constexpr int BYTES = SLOTS * ((ENGINE == kPhilox) ? 16 : 8);
+};
+
+// All NT threads of the CTA must call together; e0 = event of thread 0.  Near the end of the
+// 2^64 counter range the Philox carry into the high counter word differs between neighbouring
+// events, so there each thread computes its own blocks (a CTA-uniform branch).
+template <int N, int ENGINE, int NT>
+__device__ __forceinline__ void cta_event_words(uint64_t key, uint64_t e0, void* smem, uint64_t (&w)[3 * N - 4])
+{
+    using S = WordShare<N, ENGINE, NT>;
+    const int t = threadIdx.x;
+    if constexpr (ENGINE == kPhilox) {
+        ulonglong2* slots = static_cast<ulonglong2*>(smem);
+        const uint64_t c_first = e0 + 3u * N + 1u;                 // counter of slot 0
+        if (e0 <= ~uint64_t(0) - (3u * N + S::SLOTS)) {            // no counter of the CTA wraps
+            {
+                uint64_t o0, o1;
+                philox2x64_7(c_first + t, 0, key, o0, o1);
+                slots[t] = make_ulonglong2(o0, o1);
+            }
+            if (t < S::B - 1) {
+                uint64_t o0, o1;
+                philox2x64_7(c_first + NT + t, 0, key, o0, o1);
+                slots[NT + t] = make_ulonglong2(o0, o1);
+            }
+            __syncthreads();
+#pragma unroll
+            for (int b = 0; b < S::B; ++b) {
+                const ulonglong2 v = slots[t + b];
+                w[2 * b] = v.x;
+                if (2 * b + 1 < S::NW) w[2 * b + 1] = v.y;
+            }
+            __syncthreads();
+        } else {
+            event_words<N, kPhilox>(key, e0 + t, w);
+        }
+    } else {
+        uint64_t* slots = static_cast<uint64_t*>(smem);
+        const uint64_t c_first = e0 + 3u * N;                      // squares3 counters wrap with no carry
+        slots[t] = squares3_word(key, c_first + t);
+        if (t < S::B - 1) slots[NT + t] = squares3_word(key, c_first + NT + t);
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < S::NW; ++k) w[k] = slots[t + k];
+        __syncthreads();
+    }
+}
+
+}  // namespace hps

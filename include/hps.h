@@ -209,6 +209,59 @@ hps_status hps_unweight_flags(int32_t n_daughters, const double* masses, double 
 hps_status hps_rng_words(int32_t n_daughters, int32_t engine, uint64_t seed, uint64_t first_evt,
                          uint64_t n, uint64_t* out, void* stream);
 
+/* ------------------------------------------------- batched channels, one persistent launch -- */
+
+/* Many decay channels of different N and event counts in one persistent kernel (FP32_FIX
+ * arithmetic).  There is no single reference call for this: it batches what would be one
+ * PhaseSpace::Generate or AverageOn call per channel (PhaseSpace.inl:255-444).  Each item's
+ * results are bit-identical to the same request made alone with hps_generate / hps_average_on
+ * at HPS_PREC_FP32_FIX: the work units are the same functions of (channel, event index). */
+typedef enum hps_batch_mode { HPS_MODE_STORE = 0, HPS_MODE_AVERAGE = 1 } hps_batch_mode;
+
+typedef struct hps_batch_item {
+    hps_channel channel;
+    uint64_t first_evt;
+    uint64_t n_events;
+    int32_t mode;                        /* hps_batch_mode                                   */
+    int32_t reserved;
+    hps_functor functor;                 /* AVERAGE                                          */
+    double* cols[HPS_MAX_DAUGHTERS];     /* STORE: device columns, 16-byte aligned           */
+    double* weights;                     /* STORE: optional generation-time weights          */
+    uint8_t* flags;                      /* STORE: optional unweight flags                   */
+    uint64_t unweight_seed;              /* STORE: seed of the unweight uniforms             */
+    hps_stats* stats;                    /* AVERAGE: device output {mean, M2, W}             */
+} hps_batch_item;
+
+/* Launch shape of the persistent kernel: grid = ctas_per_sm x SM count CTAs of 256 threads;
+ * store items are cut into work units of store_tile_events events (a multiple of 256),
+ * AverageOn items into tiles of HPS_AVG_TILE events. */
+typedef struct hps_batch_tuning {
+    int32_t ctas_per_sm;
+    int32_t store_tile_events;
+} hps_batch_tuning;
+
+typedef struct hps_batch_plan hps_batch_plan;
+
+/* A plan owns the device item table (max_items entries), the AverageOn tile partials
+ * (max_average_tiles x 24 bytes), a pinned staging copy of the table and the instantiated
+ * CUDA graph (counter reset + persistent kernel + per-item merge).  tuning = NULL picks the
+ * default shape; hps_batch_autotune chooses one by timing. */
+hps_status hps_batch_create(hps_batch_plan** plan, int32_t max_items, uint64_t max_average_tiles,
+                            int32_t precision, const hps_batch_tuning* tuning);
+/* Validates the items and uploads the table asynchronously on `stream`. */
+hps_status hps_batch_set_items(hps_batch_plan* plan, const hps_batch_item* items, int32_t n_items,
+                               void* stream);
+/* One graph launch over the current items, asynchronous on `stream`. */
+hps_status hps_batch_launch(hps_batch_plan* plan, void* stream);
+hps_status hps_batch_get_tuning(const hps_batch_plan* plan, hps_batch_tuning* out);
+hps_status hps_batch_set_tuning(hps_batch_plan* plan, const hps_batch_tuning* tuning);
+/* Times candidate launch shapes on the current items (each run writes the items' outputs) and
+ * keeps the fastest; with cache_path, results are read from / appended to that text file,
+ * keyed by device, precision and the item mix.  Synchronous. */
+hps_status hps_batch_autotune(hps_batch_plan* plan, void* stream, const char* cache_path,
+                              hps_batch_tuning* chosen);
+hps_status hps_batch_destroy(hps_batch_plan* plan);
+
 /* ------------------------------------------------------------------ misc -- */
 
 const char* hps_last_error(void);
