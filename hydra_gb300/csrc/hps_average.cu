@@ -49,9 +49,18 @@ k_average_tiles_f32fix(DevChannel chd, DevChannelF ch, DevFunctor fn, uint64_t f
 {
     __shared__ __align__(16) unsigned char smem[WordShare<N, ENGINE, kAvgThreads>::BYTES];
     for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const hps_stats r = average_tile_f32<N, ENGINE>(chd, ch, fn, first, n, t, smem);
-        if (threadIdx.x == 0) partials[t] = r;
+        const hps_sums r = average_tile_f32<N, ENGINE>(chd, ch, fn, first, n, t, smem);
+        if (threadIdx.x == 0) reinterpret_cast<hps_sums*>(partials)[t] = r;
     }
+}
+
+template <int N, int ENGINE>
+__global__ void __launch_bounds__(kFinalThreads)
+k_average_final_f32fix(DevChannel chd, DevChannelF ch, DevFunctor fn, uint64_t first,
+                       const hps_stats* __restrict__ partials, uint64_t ntiles, hps_stats* __restrict__ out)
+{
+    const hps_stats r = merge_sums<N, ENGINE>(chd, ch, fn, first, partials, ntiles);
+    if (threadIdx.x == 0) *out = r;
 }
 
 // One CTA: thread j folds partials j, j+1024, ... in order, then the fixed CTA tree.
@@ -98,7 +107,16 @@ hps_status launch_average(const hps_channel* channel, const DevChannel& ch, cons
 #undef HPS_BODY
         }
     }
-    k_average_final<<<1, kFinalThreads, 0, stream>>>(partials, ntiles, out);
+    if (precision == HPS_PREC_FP32_FIX) {
+        DevChannelF chf;
+        to_device_channel_f(channel, &chf);
+#define HPS_BODY(NN, EE)                                                                                   \
+        k_average_final_f32fix<NN, EE><<<1, kFinalThreads, 0, stream>>>(ch, chf, fn, first_evt, partials, ntiles, out);
+        HPS_DISPATCH_N_ENGINE(channel->n_daughters, channel->engine, HPS_BODY)
+#undef HPS_BODY
+    } else {
+        k_average_final<<<1, kFinalThreads, 0, stream>>>(partials, ntiles, out);
+    }
     return cuda_status(cudaGetLastError(), "hps_average_on launch");
 }
 

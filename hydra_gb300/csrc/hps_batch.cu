@@ -58,8 +58,8 @@ __device__ __forceinline__ void run_unit(const BatchItemDev& it, uint64_t u, int
             store_chunk_f32<N, ENGINE>(it.chd, it.chf, it.cols, it.weights, it.flags, it.ukey, it.first, hi, cb,
                                        it.vec32 != 0, smem);
     } else {
-        const hps_stats r = average_tile_f32<N, ENGINE>(it.chd, it.chf, it.fn, it.first, it.n, u, smem);
-        if (threadIdx.x == 0) partials[it.partial_offset + u] = r;
+        const hps_sums r = average_tile_f32<N, ENGINE>(it.chd, it.chf, it.fn, it.first, it.n, u, smem);
+        if (threadIdx.x == 0) reinterpret_cast<hps_sums*>(partials)[it.partial_offset + u] = r;
     }
 }
 
@@ -101,7 +101,7 @@ k_batch_f32(const BatchItemDev* __restrict__ items, BatchHeader* __restrict__ hd
     }
 }
 
-// One CTA per item slot: AverageOn items merge their tile partials exactly as hps_average_on.
+// One CTA per item slot: AverageOn items add their tile sums exactly as hps_average_on does.
 __global__ void __launch_bounds__(kFinalThreads)
 k_batch_merge(const BatchItemDev* __restrict__ items, const BatchHeader* __restrict__ hdr,
               const hps_stats* __restrict__ partials)
@@ -109,7 +109,18 @@ k_batch_merge(const BatchItemDev* __restrict__ items, const BatchHeader* __restr
     if ((int)blockIdx.x >= hdr->n_items) return;
     const BatchItemDev& it = items[blockIdx.x];
     if (it.mode != HPS_MODE_AVERAGE) return;
-    const hps_stats r = merge_partials(partials + it.partial_offset, it.units);
+    hps_stats r{0.0, 0.0, 0.0};
+    switch (it.N * 2 + it.engine) {
+#define HPS_MERGE(NN)                                                                                        \
+    case NN * 2 + 0: r = merge_sums<NN, kPhilox>(it.chd, it.chf, it.fn, it.first, partials + it.partial_offset,  \
+                                                 it.units); break;                                            \
+    case NN * 2 + 1: r = merge_sums<NN, kSquares3>(it.chd, it.chf, it.fn, it.first,                            \
+                                                   partials + it.partial_offset, it.units); break;
+    HPS_MERGE(2) HPS_MERGE(3) HPS_MERGE(4) HPS_MERGE(5) HPS_MERGE(6) HPS_MERGE(7) HPS_MERGE(8) HPS_MERGE(9)
+    HPS_MERGE(10)
+#undef HPS_MERGE
+    default: break;
+    }
     if (threadIdx.x == 0) *it.stats = r;
 }
 

@@ -1,8 +1,9 @@
 // tiles_f32.cuh -- FP32_FIX work units shared by the single-channel kernels and the batched
 // persistent kernel, so that a channel produces bit-identical results alone or in a batch.
 //   store_chunk_f32:   NT consecutive events of a channel -> Decays columns, weight, flag
-//   average_tile_f32:  one AverageOn tile (HPS_AVG_TILE events) -> its StatsPHSP (thread 0)
-//   merge_partials:    the fixed-shape merge of a channel's tile partials
+//   average_tile_f32:  one AverageOn tile (HPS_AVG_TILE events) -> its shifted weighted sums
+//   merge_sums:        the fixed-shape sum of a call's tile sums -> its StatsPHSP
+//   merge_partials:    the fixed-shape StatsPHSP merge of the FP64 form's tile partials
 #pragma once
 #include "common.h"
 #include "store.cuh"
@@ -51,18 +52,79 @@ __device__ __forceinline__ void ff_add(float& sh, float& sl, float xh, float xl)
     sh = t;
 }
 
+// Weighted sums of one AverageOn tile relative to a shift K0 common to the whole call:
+// W = sum w, S1 = sum w (f - K0), S2 = sum w (f - K0)^2.  Tiles combine by addition, and
+// {K0 + S1/W, S2 - S1^2/W, W} is the call's StatsPHSP (StatsPHSP.h:38-86) in closed form.
+// Stored in the 24-byte partial slot of a tile.
+struct hps_sums {
+    double s1, s2, w;
+};
+static_assert(sizeof(hps_sums) == sizeof(hps_stats), "partials hold either form");
+
+__device__ __forceinline__ hps_sums shfl_down_sums(const hps_sums& s, int offset)
+{
+    return hps_sums{__shfl_down_sync(0xffffffffu, s.s1, offset), __shfl_down_sync(0xffffffffu, s.s2, offset),
+                    __shfl_down_sync(0xffffffffu, s.w, offset)};
+}
+
+// Fixed-shape CTA tree of additions (NT a multiple of 32, <= 1024); result valid in thread 0.
+template <int NT>
+__device__ __forceinline__ hps_sums block_reduce_sums(hps_sums s)
+{
+    constexpr int NWARP = NT / 32;
+    __shared__ hps_sums warp_part[NWARP];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const hps_sums o = shfl_down_sums(s, off);
+        s.s1 += o.s1; s.s2 += o.s2; s.w += o.w;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) warp_part[warp] = s;
+    __syncthreads();
+    if (warp == 0) {
+        hps_sums t = (lane < NWARP) ? warp_part[lane] : hps_sums{0.0, 0.0, 0.0};
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const hps_sums o = shfl_down_sums(t, off);
+            t.s1 += o.s1; t.s2 += o.s2; t.w += o.w;
+        }
+        s = t;
+    }
+    __syncthreads();
+    return s;
+}
+
+// The shift K0: the functor value of the call's first event, computed by thread 0 and handed
+// to every thread of the CTA.
+template <int N, int ENGINE>
+__device__ __forceinline__ float shift_value(const DevChannel& chd, const DevChannelF& ch, const DevFunctor& fn,
+                                             uint64_t first)
+{
+    __shared__ float s_k0;
+    if (threadIdx.x == 0) {
+        uint64_t w[3 * N - 4];
+        event_words<N, ENGINE>(chd.key, first, w);
+        float p[N][4];
+        f32::event_from_words<N, ENGINE>(chd, ch, w, p);
+        s_k0 = f32::functor<N>(fn, p);
+    }
+    __syncthreads();
+    const float k0 = s_k0;
+    __syncthreads();
+    return k0;
+}
+
 // AverageOn tile t: thread j takes events t*4096 + j + 256k, k = 0..15, and accumulates their
 // prod(pdk) P (the weight without the common factor max_weight) as float-float sums
-// W' = sum P, S1' = sum P (f - K), S2' = sum P (f - K)^2 with K its first functor value -- the
-// StatsPHSP of those events in closed form once scaled by max_weight in double; the fixed
-// warp/CTA tree then merges the per-thread StatsPHSP.  Result valid in thread 0.
+// sum P, sum P (f - K0), sum P (f - K0)^2, converted to double and scaled by max_weight; the
+// fixed CTA tree adds the per-thread sums.  Result valid in thread 0.
 template <int N, int ENGINE>
-__device__ __forceinline__ hps_stats average_tile_f32(const DevChannel& chd, const DevChannelF& ch,
-                                                      const DevFunctor& fn, uint64_t first, uint64_t n,
-                                                      uint64_t t, void* smem)
+__device__ __forceinline__ hps_sums average_tile_f32(const DevChannel& chd, const DevChannelF& ch,
+                                                     const DevFunctor& fn, uint64_t first, uint64_t n,
+                                                     uint64_t t, void* smem)
 {
+    const float K0 = shift_value<N, ENGINE>(chd, ch, fn, first);
     float swh = 0.0f, swl = 0.0f, s1h = 0.0f, s1l = 0.0f, s2h = 0.0f, s2l = 0.0f;
-    float K = 0.0f;
     const uint64_t base = t * HPS_AVG_TILE;
     for (int k = 0; k < kAvgPerThread; ++k) {
         const uint64_t cb = base + (uint64_t)k * kTileThreads;
@@ -73,9 +135,7 @@ __device__ __forceinline__ hps_stats average_tile_f32(const DevChannel& chd, con
         if (e < n) {
             float p[N][4];
             const f32::EventWeight ew = f32::event_from_words<N, ENGINE>(chd, ch, w, p);
-            const float f = f32::functor<N>(fn, p);
-            if (k == 0) K = f;
-            const float d = f - K;
+            const float d = f32::functor<N>(fn, p) - K0;
             // P*d and P*d^2 as float-float products
             const float h1 = ew.prod_hi * d;
             const float l1 = fmaf(ew.prod_lo, d, fmaf(ew.prod_hi, d, -h1));
@@ -86,17 +146,36 @@ __device__ __forceinline__ hps_stats average_tile_f32(const DevChannel& chd, con
             ff_add(s2h, s2l, h2, l2);
         }
     }
-    hps_stats acc{0.0, 0.0, 0.0};
-    const double W = chd.max_weight * (f32::widen(swh) + f32::widen(swl));
-    if (W != 0.0) {
-        const double S1 = chd.max_weight * (f32::widen(s1h) + f32::widen(s1l));
-        const double S2 = chd.max_weight * (f32::widen(s2h) + f32::widen(s2l));
-        const double q = S1 / W;
-        acc.w = W;
-        acc.mean = f32::widen(K) + q;
-        acc.m2 = fma(-S1, q, S2);
+    hps_sums acc;
+    acc.w = chd.max_weight * (f32::widen(swh) + f32::widen(swl));
+    acc.s1 = chd.max_weight * (f32::widen(s1h) + f32::widen(s1l));
+    acc.s2 = chd.max_weight * (f32::widen(s2h) + f32::widen(s2l));
+    return block_reduce_sums<kTileThreads>(acc);
+}
+
+// Thread j of a kFinalThreads CTA adds tile sums j, j+1024, ... in order, the fixed CTA tree adds
+// the threads' sums, and the call's StatsPHSP is formed from them.  Result valid in thread 0.
+template <int N, int ENGINE>
+__device__ __forceinline__ hps_stats merge_sums(const DevChannel& chd, const DevChannelF& ch, const DevFunctor& fn,
+                                                uint64_t first, const hps_stats* __restrict__ partials,
+                                                uint64_t ntiles)
+{
+    const hps_sums* tiles = reinterpret_cast<const hps_sums*>(partials);
+    hps_sums acc{0.0, 0.0, 0.0};
+    for (uint64_t t = threadIdx.x; t < ntiles; t += kFinalThreads) {
+        const hps_sums v = tiles[t];
+        acc.s1 += v.s1; acc.s2 += v.s2; acc.w += v.w;
     }
-    return block_reduce_stats<kTileThreads>(acc);
+    const hps_sums tot = block_reduce_sums<kFinalThreads>(acc);
+    const float K0 = (ntiles > 0) ? shift_value<N, ENGINE>(chd, ch, fn, first) : 0.0f;
+    hps_stats r{0.0, 0.0, 0.0};
+    if (tot.w != 0.0) {
+        const double q = tot.s1 / tot.w;
+        r.w = tot.w;
+        r.mean = f32::widen(K0) + q;
+        r.m2 = fma(-tot.s1, q, tot.s2);
+    }
+    return r;
 }
 
 // Thread j of a kFinalThreads CTA folds partials j, j+1024, ... in order, then the fixed CTA

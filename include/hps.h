@@ -262,6 +262,73 @@ hps_status hps_batch_autotune(hps_batch_plan* plan, void* stream, const char* ca
                               hps_batch_tuning* chosen);
 hps_status hps_batch_destroy(hps_batch_plan* plan);
 
+/* ------------------------------------------------------------ serving loop -- */
+
+/* A request server with continuous batching: requests (Generate-into-Decays or AverageOn of
+ * one channel) are submitted from any host thread, admitted in arrival order while their
+ * output memory fits the device budget, and run by a scheduler thread as batched persistent
+ * launches (hps_batch_*).  A launch takes every admitted request that still has work, store
+ * requests in slices of at most slice_events events, so requests that arrive while others are
+ * on the GPU join the next launch and run alongside them.  Results are bit-identical to the
+ * same request run alone with hps_generate / hps_average_on at HPS_PREC_FP32_FIX.
+ * The channel table and each request's event counters live in the device item table of the
+ * launch.  No reference counterpart: Hydra runs one blocking call per request. */
+typedef struct hps_server hps_server;
+typedef uint64_t hps_ticket;
+
+typedef struct hps_server_config {
+    uint64_t budget_bytes;       /* device bytes for request outputs (store columns etc.)    */
+    uint64_t slice_events;       /* max events of one store request per launch (0: 2^22)    */
+    int32_t max_batch_items;     /* items per launch (0: 1024)                              */
+    int32_t max_inflight;        /* admitted requests not yet released (0: 4096)            */
+    uint64_t max_average_events; /* AverageOn events per launch (0: 2^30)                   */
+    int32_t fail_alloc_after;    /* test hook: the n-th output allocation fails (0: never)  */
+    int32_t reserved;
+} hps_server_config;
+
+typedef struct hps_request {
+    hps_channel channel;
+    uint64_t first_evt;
+    uint64_t n_events;
+    int32_t mode;                /* HPS_MODE_STORE or HPS_MODE_AVERAGE                      */
+    int32_t want_flags;          /* store: also produce unweight flags                      */
+    hps_functor functor;         /* AverageOn                                               */
+    uint64_t unweight_seed;
+} hps_request;
+
+typedef struct hps_result {
+    int32_t status;              /* HPS_OK, or the error that ended the request             */
+    int32_t mode;
+    uint64_t n_events;
+    double* cols[HPS_MAX_DAUGHTERS];   /* store: device columns, valid until hps_server_release */
+    double* weights;             /* store: generation-time weights                          */
+    uint8_t* flags;              /* store: unweight flags, if requested                     */
+    hps_stats stats;             /* AverageOn: {mean, M2, W}                                */
+    double t_submit, t_admit, t_done;  /* seconds on the server's steady clock              */
+} hps_result;
+
+typedef struct hps_server_stats {
+    uint64_t submitted, admitted, completed, cancelled, failed, released;
+    uint64_t launches, events_done;
+    uint64_t bytes_in_use, bytes_peak;
+} hps_server_stats;
+
+/* Starts the scheduler thread on the current device. */
+hps_status hps_server_create(hps_server** server, const hps_server_config* config);
+/* Queues a request (thread-safe, non-blocking).  HPS_ERR_BUDGET if it can never fit. */
+hps_status hps_server_submit(hps_server* server, const hps_request* request, hps_ticket* ticket);
+/* *done = 1 and *result filled once the request has finished (or failed / been cancelled). */
+hps_status hps_server_poll(hps_server* server, hps_ticket ticket, hps_result* result, int32_t* done);
+/* Waits at most timeout_s seconds; HPS_ERR_TIMEOUT if the request is still running. */
+hps_status hps_server_wait(hps_server* server, hps_ticket ticket, hps_result* result, double timeout_s);
+/* Cancels a request that has not been admitted yet (HPS_ERR_BAD_ARG once it runs). */
+hps_status hps_server_cancel(hps_server* server, hps_ticket ticket);
+/* Returns a finished request's output memory to the budget; the ticket becomes invalid. */
+hps_status hps_server_release(hps_server* server, hps_ticket ticket);
+hps_status hps_server_get_stats(hps_server* server, hps_server_stats* stats);
+/* Stops the scheduler after the running launches finish; queued requests are cancelled. */
+hps_status hps_server_destroy(hps_server* server);
+
 /* ------------------------------------------------------------------ misc -- */
 
 const char* hps_last_error(void);

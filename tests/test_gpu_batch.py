@@ -132,7 +132,6 @@ def test_batch_against_oracle(api, torch, oracle):
     torch.cuda.synchronize()
     for r in mix:
         ch, first, n = r[1], r[2], r[3]
-        och = oracle.make_channel(list(ch.masses)[:ch.n_daughters], 0, 0)  # placeholder, replaced below
         och = oracle.Channel()
         for f in ("n_daughters", "engine", "seed", "ecm", "max_weight"):
             setattr(och, f, getattr(ch, f))
