@@ -80,6 +80,51 @@ class HpsBatchTuning(ctypes.Structure):
 MODE_STORE, MODE_AVERAGE = 0, 1
 
 
+class HpsServerConfig(ctypes.Structure):
+    _fields_ = [
+        ("budget_bytes", ctypes.c_uint64),
+        ("slice_events", ctypes.c_uint64),
+        ("max_batch_items", ctypes.c_int32),
+        ("max_inflight", ctypes.c_int32),
+        ("max_average_events", ctypes.c_uint64),
+        ("fail_alloc_after", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+    ]
+
+
+class HpsRequest(ctypes.Structure):
+    _fields_ = [
+        ("channel", HpsChannel),
+        ("first_evt", ctypes.c_uint64),
+        ("n_events", ctypes.c_uint64),
+        ("mode", ctypes.c_int32),
+        ("want_flags", ctypes.c_int32),
+        ("functor", HpsFunctor),
+        ("unweight_seed", ctypes.c_uint64),
+    ]
+
+
+class HpsResult(ctypes.Structure):
+    _fields_ = [
+        ("status", ctypes.c_int32),
+        ("mode", ctypes.c_int32),
+        ("n_events", ctypes.c_uint64),
+        ("cols", ctypes.c_void_p * HPS_MAX_DAUGHTERS),
+        ("weights", ctypes.c_void_p),
+        ("flags", ctypes.c_void_p),
+        ("stats", HpsStats),
+        ("t_submit", ctypes.c_double),
+        ("t_admit", ctypes.c_double),
+        ("t_done", ctypes.c_double),
+    ]
+
+
+class HpsServerStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in ("submitted", "admitted", "completed", "cancelled", "failed",
+                                                 "released", "launches", "events_done", "bytes_in_use",
+                                                 "bytes_peak")]
+
+
 class HpsError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"hps status {status}: {message}")
@@ -101,6 +146,8 @@ SIGNATURES = {
                                       _i32, _vp]),
     "hps_event_weights": (_i32, [_i32, _vp, _dbl, _u64, _vp, _vp, _vp]),
     "hps_unweight_flags": (_i32, [_i32, _vp, _dbl, _u64, _vp, _u64, _u64, _vp, _vp]),
+    "hps_compact_workspace_size": (_sz, [_u64]),
+    "hps_unweight_compact": (_i32, [_i32, _u64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "hps_rng_words": (_i32, [_i32, _i32, _u64, _u64, _u64, _vp, _vp]),
     "hps_default_seed": (_u64, [_i32, _vp]),
     "hps_batch_create": (_i32, [_vp, _i32, _u64, _i32, _vp]),
@@ -110,6 +157,15 @@ SIGNATURES = {
     "hps_batch_set_tuning": (_i32, [_vp, _vp]),
     "hps_batch_autotune": (_i32, [_vp, _vp, ctypes.c_char_p, _vp]),
     "hps_batch_destroy": (_i32, [_vp]),
+    "hps_server_create": (_i32, [_vp, ctypes.POINTER(HpsServerConfig)]),
+    "hps_server_submit": (_i32, [_vp, ctypes.POINTER(HpsRequest), ctypes.POINTER(ctypes.c_uint64)]),
+    "hps_server_poll": (_i32, [_vp, _u64, ctypes.POINTER(HpsResult), ctypes.POINTER(ctypes.c_int32)]),
+    "hps_server_wait": (_i32, [_vp, _u64, ctypes.POINTER(HpsResult), _dbl]),
+    "hps_server_next_done": (_i32, [_vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(HpsResult), _dbl]),
+    "hps_server_cancel": (_i32, [_vp, _u64]),
+    "hps_server_release": (_i32, [_vp, _u64]),
+    "hps_server_get_stats": (_i32, [_vp, ctypes.POINTER(HpsServerStats)]),
+    "hps_server_destroy": (_i32, [_vp]),
     "hps_last_error": (ctypes.c_char_p, []),
     "hps_abi_version": (_i32, []),
 }

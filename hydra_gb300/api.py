@@ -20,8 +20,9 @@ from typing import Iterable, Sequence
 import torch
 
 from . import (
-    MODE_AVERAGE, MODE_STORE, HpsBatchItem, HpsBatchTuning,
-    DEFAULT_UNWEIGHT_SEED, ENGINE_PHILOX, ENGINE_SQUARES3, ERR_BAD_ARG, ERR_NO_ENERGY, FN_BW2, FN_MASS2, FN_ONE,
+    MODE_AVERAGE, MODE_STORE, HpsBatchItem, HpsBatchTuning, HpsRequest, HpsResult, HpsServerConfig,
+    HpsServerStats,
+    DEFAULT_UNWEIGHT_SEED, ENGINE_PHILOX, ENGINE_SQUARES3, ERR_BAD_ARG, ERR_NO_ENERGY, ERR_TIMEOUT, FN_BW2, FN_MASS2, FN_ONE,
     HPS_MAX_DAUGHTERS, PREC_FP32_FIX, PREC_FP64, HpsChannel, HpsError, HpsFunctor, check, lib,
 )
 
@@ -189,6 +190,22 @@ def unweight_flags(n_daughters: int, masses: Sequence[float], max_weight: float,
                                    _dptr(flags), _stream_handle(stream)))
 
 
+def unweight_compact(four: torch.Tensor, flags: torch.Tensor, weights: torch.Tensor | None = None,
+                     stream=None):
+    """Stable partition of stored events by flags (accepted first): returns (four_out,
+    weights_out or None, n_accepted as a 1-element int64 CUDA tensor)."""
+    N, n = four.shape[0], four.shape[1]
+    out = torch.empty_like(four)
+    wout = torch.empty_like(weights) if weights is not None else None
+    nacc = torch.zeros(1, dtype=torch.int64, device=four.device)
+    cin = _ptr_array([four[k] for k in range(N)])
+    cout = _ptr_array([out[k] for k in range(N)])
+    check(lib().hps_unweight_compact(N, n, ctypes.cast(cin, ctypes.c_void_p), _dptr(weights), _dptr(flags),
+                                     ctypes.cast(cout, ctypes.c_void_p), _dptr(wout), _dptr(nacc), None, 0,
+                                     _stream_handle(stream)))
+    return out, wout, nacc
+
+
 def rng_words(n_daughters: int, engine, seed: int, first: int, n: int, out: torch.Tensor, stream=None) -> None:
     if out.dtype not in (torch.int64, torch.uint64) or out.numel() < n * (3 * n_daughters - 4):
         raise ValueError("out must be 64-bit with n*(3N-4) elements")
@@ -270,6 +287,108 @@ class BatchPlan:
             pass
 
 
+# ----------------------------------------------------------------------------- serving loop
+
+def store_request(ch: HpsChannel, first: int, n: int, want_flags: bool = False,
+                  unweight_seed: int = DEFAULT_UNWEIGHT_SEED) -> HpsRequest:
+    r = HpsRequest()
+    r.channel = ch
+    r.first_evt = first
+    r.n_events = n
+    r.mode = MODE_STORE
+    r.want_flags = 1 if want_flags else 0
+    r.unweight_seed = unweight_seed & (2**64 - 1)
+    return r
+
+
+def average_request(ch: HpsChannel, first: int, n: int, functor: HpsFunctor) -> HpsRequest:
+    r = HpsRequest()
+    r.channel = ch
+    r.first_evt = first
+    r.n_events = n
+    r.mode = MODE_AVERAGE
+    r.functor = functor
+    return r
+
+
+class Server:
+    """Continuous-batching request server (hps_server_*)."""
+
+    def __init__(self, budget_bytes: int, slice_events: int = 0, max_batch_items: int = 0, max_inflight: int = 0,
+                 max_average_events: int = 0, fail_alloc_after: int = 0):
+        cfg = HpsServerConfig(budget_bytes, slice_events, max_batch_items, max_inflight, max_average_events,
+                              fail_alloc_after, 0)
+        self._s = ctypes.c_void_p()
+        check(lib().hps_server_create(ctypes.byref(self._s), ctypes.byref(cfg)))
+
+    def submit(self, request: HpsRequest) -> int:
+        t = ctypes.c_uint64()
+        check(lib().hps_server_submit(self._s, ctypes.byref(request), ctypes.byref(t)))
+        return t.value
+
+    def poll(self, ticket: int):
+        res = HpsResult()
+        done = ctypes.c_int32()
+        check(lib().hps_server_poll(self._s, ticket, ctypes.byref(res), ctypes.byref(done)))
+        return res if done.value else None
+
+    def wait(self, ticket: int, timeout_s: float = 60.0) -> HpsResult:
+        res = HpsResult()
+        check(lib().hps_server_wait(self._s, ticket, ctypes.byref(res), timeout_s))
+        return res
+
+    def next_done(self, timeout_s: float = 1.0):
+        """(ticket, result) of the next request to finish, or None after timeout_s."""
+        t = ctypes.c_uint64()
+        res = HpsResult()
+        st = lib().hps_server_next_done(self._s, ctypes.byref(t), ctypes.byref(res), timeout_s)
+        if st == ERR_TIMEOUT:
+            return None
+        check(st)
+        return t.value, res
+
+    def cancel(self, ticket: int) -> None:
+        check(lib().hps_server_cancel(self._s, ticket))
+
+    def release(self, ticket: int) -> None:
+        check(lib().hps_server_release(self._s, ticket))
+
+    def stats(self) -> dict:
+        st = HpsServerStats()
+        check(lib().hps_server_get_stats(self._s, ctypes.byref(st)))
+        return {n: getattr(st, n) for n, _ in HpsServerStats._fields_}
+
+    def close(self) -> None:
+        if self._s:
+            lib().hps_server_destroy(self._s)
+            self._s = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class _DeviceArray:
+    """Exposes a raw device pointer through __cuda_array_interface__ (zero-copy torch view)."""
+
+    def __init__(self, ptr: int, shape: tuple, typestr: str):
+        self.__cuda_array_interface__ = {"shape": shape, "typestr": typestr, "data": (int(ptr), False),
+                                         "version": 3, "strides": None}
+
+
+def result_views(res: HpsResult, n_daughters: int):
+    """Zero-copy torch views of a finished request's outputs: (four [N, n, 4], weights [n],
+    flags [n] or None) for a store request, valid until the request is released."""
+    n = int(res.n_events)
+    cols = [torch.as_tensor(_DeviceArray(res.cols[k], (n, 4), "<f8"), device="cuda") for k in range(n_daughters)]
+    four = torch.stack(cols) if n else torch.empty((n_daughters, 0, 4), dtype=torch.float64, device="cuda")
+    w = torch.as_tensor(_DeviceArray(res.weights, (n,), "<f8"), device="cuda") if res.weights else None
+    fl = torch.as_tensor(_DeviceArray(res.flags, (n,), "|u1"), device="cuda") if res.flags else None
+    return four, w, fl
+
+
 # ----------------------------------------------------------------------------- reference-shaped API
 
 @dataclass
@@ -345,13 +464,12 @@ class Decays:
 
     def Unweight(self, seed: int = DEFAULT_UNWEIGHT_SEED) -> int:
         """Decays::Unweight (Decays.inl:415-455): stable-partitions the accepted events to the
-        front and returns their count."""
-        flags = self.UnweightFlags(seed).bool()
-        order = torch.cat([torch.nonzero(flags).flatten(), torch.nonzero(~flags).flatten()])
-        self.four = self.four.index_select(1, order).contiguous()
+        front (hps_unweight_compact) and returns their count."""
+        flags = self.UnweightFlags(seed)
+        self.four, w, nacc = unweight_compact(self.four, flags, self.weights)
         if self.weights is not None:
-            self.weights = self.weights.index_select(0, order).contiguous()
-        return int(flags.sum().item())
+            self.weights = w
+        return int(nacc.item())
 
 
 class PhaseSpace:

@@ -21,6 +21,8 @@
 
 #include "common.h"
 
+using namespace hps;
+
 namespace {
 
 double now_s()
@@ -72,6 +74,7 @@ struct hps_server {
     hps_batch_plan* plans[2] = {nullptr, nullptr};
     int next_plan = 0;
     std::deque<Launch> inflight;
+    std::deque<hps_ticket> finished;       // completion queue for hps_server_next_done
     uint64_t launched = 0;
     std::atomic<uint64_t> completed{0};
     hps_stats* slots_host = nullptr;       // pinned, mapped: AverageOn results land here
@@ -96,12 +99,13 @@ void CUDART_CB on_launch_done(void* p)
     s->cv_sched.notify_all();
 }
 
-void fail_request(hps_server* s, Req& r, hps_status status)
+void fail_request(hps_server* s, hps_ticket t, Req& r, hps_status status)
 {
     r.state = kFailed;
     r.status = status;
     r.t_done = now_s();
     s->st.failed++;
+    s->finished.push_back(t);
 }
 
 // Called with the lock held.
@@ -124,6 +128,7 @@ void retire(hps_server* s)
             r.t_done = now_s();
             s->st.completed++;
             s->st.events_done += r.req.n_events;
+            s->finished.push_back(t);
         }
         s->inflight.pop_front();
         any = true;
@@ -160,7 +165,7 @@ void admit(hps_server* s)
                 cudaGetLastError();
                 r.buf = nullptr;
                 s->pending.pop_front();
-                fail_request(s, r, HPS_ERR_OOM);
+                fail_request(s, t, r, HPS_ERR_OOM);
                 s->cv_done.notify_all();
                 continue;
             }
@@ -262,7 +267,7 @@ bool launch(hps_server* s)
         s->fatal = stt;
         std::snprintf(s->fatal_msg, sizeof(s->fatal_msg), "%s", hps_last_error());
         for (auto& kv : s->reqs)
-            if (kv.second.state == kRunning || kv.second.state == kQueued) fail_request(s, kv.second, stt);
+            if (kv.second.state == kRunning || kv.second.state == kQueued) fail_request(s, kv.first, kv.second, stt);
         s->active.clear();
         s->pending.clear();
         s->cv_done.notify_all();
@@ -416,8 +421,32 @@ hps_status hps_server_cancel(hps_server* s, hps_ticket t)
     r.state = kCancelled;
     r.t_done = now_s();
     s->st.cancelled++;
+    s->finished.push_back(t);
     s->cv_done.notify_all();
     return HPS_OK;
+}
+
+hps_status hps_server_next_done(hps_server* s, hps_ticket* ticket, hps_result* result, double timeout_s)
+{
+    clear_error();
+    if (!s || !ticket) return set_error(HPS_ERR_BAD_ARG, "NULL argument");
+    std::unique_lock<std::mutex> lock(s->mu);
+    const auto deadline = std::chrono::steady_clock::now() +
+                          std::chrono::duration_cast<std::chrono::steady_clock::duration>(
+                              std::chrono::duration<double>(timeout_s < 0 ? 0 : timeout_s));
+    for (;;) {
+        while (!s->finished.empty()) {
+            const hps_ticket t = s->finished.front();
+            s->finished.pop_front();
+            auto it = s->reqs.find(t);
+            if (it == s->reqs.end()) continue;          // released already
+            *ticket = t;
+            if (result) fill_result(it->second, result);
+            return HPS_OK;
+        }
+        if (s->cv_done.wait_until(lock, deadline) == std::cv_status::timeout && s->finished.empty())
+            return set_error(HPS_ERR_TIMEOUT, "no request finished within %.3f s", timeout_s);
+    }
 }
 
 hps_status hps_server_release(hps_server* s, hps_ticket t)

@@ -203,6 +203,17 @@ hps_status hps_unweight_flags(int32_t n_daughters, const double* masses, double 
                               uint64_t n, const double* const* cols, uint64_t unweight_seed,
                               uint64_t first_evt, uint8_t* flags, void* stream);
 
+/* Unweight compaction: the stable_partition of Decays::Unweight() (hydra/detail/Decays.inl:444-453),
+ * out of place.  Events with flags[e] != 0 go to cols_out[.][0, A), the others to [A, n), each
+ * group in index order; *n_accepted (device pointer, may be NULL) receives A.  weights_in /
+ * weights_out (both or neither) carry the weight column along.  Scratch: workspace of at least
+ * hps_compact_workspace_size(n) bytes, or NULL for the stream-ordered allocator. */
+size_t hps_compact_workspace_size(uint64_t n);
+hps_status hps_unweight_compact(int32_t n_daughters, uint64_t n, const double* const* cols_in,
+                                const double* weights_in, const uint8_t* flags, double* const* cols_out,
+                                double* weights_out, uint64_t* n_accepted, void* workspace,
+                                size_t workspace_bytes, void* stream);
+
 /* Raw random words of each event's stream (parity instrument): out[e*(3N-4)+k] is the k-th
  * word the reference engine returns for event first_evt+e (EngineR123.h:149-166 returns 64-bit
  * Philox words; squares3.h:105-119 returns 32-bit words, stored zero-extended). */
@@ -321,6 +332,9 @@ hps_status hps_server_submit(hps_server* server, const hps_request* request, hps
 hps_status hps_server_poll(hps_server* server, hps_ticket ticket, hps_result* result, int32_t* done);
 /* Waits at most timeout_s seconds; HPS_ERR_TIMEOUT if the request is still running. */
 hps_status hps_server_wait(hps_server* server, hps_ticket ticket, hps_result* result, double timeout_s);
+/* Completion queue: hands out finished requests in the order they finished, each once;
+ * waits at most timeout_s seconds (HPS_ERR_TIMEOUT when none finished). */
+hps_status hps_server_next_done(hps_server* server, hps_ticket* ticket, hps_result* result, double timeout_s);
 /* Cancels a request that has not been admitted yet (HPS_ERR_BAD_ARG once it runs). */
 hps_status hps_server_cancel(hps_server* server, hps_ticket ticket);
 /* Returns a finished request's output memory to the budget; the ticket becomes invalid. */

@@ -1,0 +1,542 @@
+/*
+ * hps_phasespace.hpp -- C++ drop-in for Hydra's phase-space classes over the libhps C ABI.
+ *
+ * Mirrors the public interface of the reference for this path, so code written against
+ *   hydra::PhaseSpace<N,GRND>   (hydra/PhaseSpace.h:86-346, hydra/detail/PhaseSpace.inl)
+ *   hydra::Decays<tuple<P...>,Backend>  (hydra/Decays.h:67-651, hydra/detail/Decays.inl)
+ *   hydra::Vector4R             (hydra/Vector4R.h:59-138)
+ * compiles against these headers (put <repo>/include first on the include path, link with
+ * libhps.so and the CUDA runtime).  Calls block like the reference's Thrust algorithms.
+ * Constructors throw std::invalid_argument / std::runtime_error with the reference's messages;
+ * CUDA failures throw std::system_error.
+ *
+ * What crosses the C ABI is the functor menu of hps.h: AverageOn / Evaluate take
+ * hydra::hps_fn::One, Mass2(i, j) or BW2(i, j, mass, width) instead of an arbitrary lambda.
+ * hydra::Decays stores the generation-time weight beside the four-vectors (the reference
+ * drops it, DecayMother.h:285); Unweight() reorders accepted events to the front.
+ */
+#ifndef HYDRA_HPS_PHASESPACE_HPP_
+#define HYDRA_HPS_PHASESPACE_HPP_
+
+#include <cuda_runtime_api.h>
+
+#include <array>
+#include <cmath>
+#include <cstddef>
+#include <cstdint>
+#include <functional>
+#include <initializer_list>
+#include <ostream>
+#include <stdexcept>
+#include <string>
+#include <system_error>
+#include <tuple>
+#include <type_traits>
+#include <utility>
+#include <vector>
+
+#include "../hps.h"
+
+namespace hydra {
+
+typedef double GReal_t;
+typedef int GInt_t;
+typedef unsigned int GUInt_t;
+typedef long GLong_t;
+
+template <typename... T> using tuple = std::tuple<T...>;
+using std::get;
+using std::make_tuple;
+
+// ---------------------------------------------------------------------------------- Vector4R
+
+class Vector4R {
+public:
+    Vector4R() = default;
+    Vector4R(GReal_t e, GReal_t px, GReal_t py, GReal_t pz) : v_{e, px, py, pz} {}
+    GReal_t get(GInt_t i) const { return v_[i]; }
+    void set(GInt_t i, GReal_t d) { v_[i] = d; }
+    void set(GReal_t e, GReal_t px, GReal_t py, GReal_t pz) { v_[0] = e; v_[1] = px; v_[2] = py; v_[3] = pz; }
+    GReal_t mass2() const { return v_[0] * v_[0] - v_[1] * v_[1] - v_[2] * v_[2] - v_[3] * v_[3]; }
+    GReal_t mass() const { const GReal_t m2 = mass2(); return m2 > 0.0 ? std::sqrt(m2) : 0.0; }
+    GReal_t d3mag() const { return std::sqrt(v_[1] * v_[1] + v_[2] * v_[2] + v_[3] * v_[3]); }
+    Vector4R& operator+=(const Vector4R& o) { for (int i = 0; i < 4; ++i) v_[i] += o.v_[i]; return *this; }
+    Vector4R& operator-=(const Vector4R& o) { for (int i = 0; i < 4; ++i) v_[i] -= o.v_[i]; return *this; }
+    Vector4R& operator*=(GReal_t c) { for (int i = 0; i < 4; ++i) v_[i] *= c; return *this; }
+    friend Vector4R operator+(Vector4R a, const Vector4R& b) { return a += b; }
+    friend Vector4R operator-(Vector4R a, const Vector4R& b) { return a -= b; }
+    friend Vector4R operator*(GReal_t c, Vector4R a) { return a *= c; }
+    friend Vector4R operator*(Vector4R a, GReal_t c) { return a *= c; }
+    // Minkowski product E1 E2 - p1.p2
+    friend GReal_t operator*(const Vector4R& a, const Vector4R& b)
+    {
+        return a.v_[0] * b.v_[0] - a.v_[1] * b.v_[1] - a.v_[2] * b.v_[2] - a.v_[3] * b.v_[3];
+    }
+    friend std::ostream& operator<<(std::ostream& s, const Vector4R& v)
+    {
+        return s << "(" << v.v_[0] << "," << v.v_[1] << "," << v.v_[2] << "," << v.v_[3] << ")";
+    }
+    const GReal_t* data() const { return v_; }
+
+private:
+    alignas(16) GReal_t v_[4] = {0.0, 0.0, 0.0, 0.0};
+};
+
+// A named argument type, as the reference's declarg (a Vector4R or a double with a name).
+namespace detail {
+template <typename T, bool = std::is_class<T>::value>
+struct arg_base : public T {
+    arg_base() = default;
+    arg_base(T const& x) : T(x) {}
+};
+template <typename T>
+struct arg_base<T, false> {
+    T value{};
+    arg_base() = default;
+    arg_base(T x) : value(x) {}
+    operator T() const { return value; }
+};
+}  // namespace detail
+
+#define declarg(NAME, TYPE)                                              \
+    struct NAME : public ::hydra::detail::arg_base<TYPE> {               \
+        using ::hydra::detail::arg_base<TYPE>::arg_base;                 \
+        NAME() = default;                                                \
+    };
+
+// ----------------------------------------------------------------------------- back-ends
+
+namespace detail {
+struct HostBackend {};
+struct DeviceBackend {};
+
+inline void throw_status(hps_status st)
+{
+    if (st == HPS_OK) return;
+    const std::string msg = hps_last_error();
+    if (st == HPS_ERR_BAD_ARG) throw std::invalid_argument(msg);
+    if (st == HPS_ERR_NO_ENERGY) throw std::runtime_error(msg);
+    throw std::system_error(std::error_code(static_cast<int>(st), std::generic_category()), msg);
+}
+
+inline void throw_cuda(cudaError_t e, const char* what)
+{
+    if (e != cudaSuccess)
+        throw std::system_error(std::error_code(static_cast<int>(e), std::generic_category()),
+                                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <typename T> struct DeviceBuffer {
+    T* p = nullptr;
+    size_t n = 0;
+    DeviceBuffer() = default;
+    explicit DeviceBuffer(size_t count) { resize(count); }
+    DeviceBuffer(const DeviceBuffer&) = delete;
+    DeviceBuffer& operator=(const DeviceBuffer&) = delete;
+    DeviceBuffer(DeviceBuffer&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    DeviceBuffer& operator=(DeviceBuffer&& o) noexcept { std::swap(p, o.p); std::swap(n, o.n); return *this; }
+    ~DeviceBuffer() { if (p) cudaFree(p); }
+    void resize(size_t count)
+    {
+        if (p) { cudaFree(p); p = nullptr; }
+        n = count;
+        void* q = nullptr;
+        if (count) throw_cuda(cudaMalloc(&q, count * sizeof(T)), "cudaMalloc");
+        p = static_cast<T*>(q);
+    }
+};
+}  // namespace detail
+
+namespace host { typedef detail::HostBackend sys_t; static const sys_t sys{}; }
+namespace device { typedef detail::DeviceBackend sys_t; static const sys_t sys{}; }
+
+// ------------------------------------------------------------------------------- engines
+
+// Engine tags: hydra::philox (EngineR123<Philox2x64>, 7 rounds) and
+// hydra::default_random_engine (squares3), as the reference's typedefs name them.
+namespace random { struct philox {}; struct squares3 {}; }
+typedef random::philox philox;
+typedef random::squares3 default_random_engine;
+
+namespace detail {
+template <typename GRND> struct engine_id;
+template <> struct engine_id<random::philox> { static constexpr int32_t value = HPS_ENGINE_PHILOX; };
+template <> struct engine_id<random::squares3> { static constexpr int32_t value = HPS_ENGINE_SQUARES3; };
+}  // namespace detail
+
+// ------------------------------------------------------------------------------ functors
+
+namespace hps_fn {
+struct One { hps_functor f{HPS_FN_ONE, 0, 1, 0, 0.0, 0.0}; };
+struct Mass2 { hps_functor f; Mass2(int i, int j) : f{HPS_FN_MASS2, i, j, 0, 0.0, 0.0} {} };
+struct BW2 { hps_functor f; BW2(int i, int j, double m, double w) : f{HPS_FN_BW2, i, j, 0, m, w} {} };
+template <typename F> struct is_menu : std::false_type {};
+template <> struct is_menu<One> : std::true_type {};
+template <> struct is_menu<Mass2> : std::true_type {};
+template <> struct is_menu<BW2> : std::true_type {};
+}  // namespace hps_fn
+
+// --------------------------------------------------------------------------------- Decays
+
+template <typename Tuple, typename Backend> class Decays;
+
+template <typename... Particles, typename Backend>
+class Decays<hydra::tuple<Particles...>, Backend> {
+public:
+    enum { nparticles = sizeof...(Particles) };
+    static_assert(nparticles >= 2 && nparticles <= HPS_MAX_DAUGHTERS, "2..10 daughters");
+    typedef hydra::tuple<Particles...> value_type;
+    static constexpr bool on_device = std::is_same<Backend, detail::DeviceBackend>::value;
+
+    Decays(double motherMass, std::array<double, nparticles> const& masses, size_t nentries = 0)
+        : fMotherMass(motherMass)
+    {
+        for (size_t i = 0; i < nparticles; ++i) fMasses[i] = masses[i];
+        init(nentries);
+    }
+    Decays(double motherMass, const double (&masses)[nparticles], size_t nentries = 0) : fMotherMass(motherMass)
+    {
+        for (size_t i = 0; i < nparticles; ++i) fMasses[i] = masses[i];
+        init(nentries);
+    }
+
+    size_t size() const { return fN; }
+    bool empty() const { return fN == 0; }
+    double GetMaxWeight() const { return fMaxWeight; }
+    double GetMotherMass() const { return fMotherMass; }
+    const std::array<double, nparticles> GetMasses() const
+    {
+        std::array<double, nparticles> a;
+        for (size_t i = 0; i < nparticles; ++i) a[i] = fMasses[i];
+        return a;
+    }
+
+    void resize(size_t n) { init(n); }
+
+    // Event i as a tuple of daughters (copied from the device for a device Decays).
+    value_type operator[](size_t i) const
+    {
+        Vector4R p[nparticles];
+        for (size_t k = 0; k < nparticles; ++k) {
+            double v[4];
+            if (on_device)
+                detail::throw_cuda(cudaMemcpy(v, column(k) + 4 * i, sizeof(v), cudaMemcpyDeviceToHost), "cudaMemcpy");
+            else
+                for (int c = 0; c < 4; ++c) v[c] = column(k)[4 * i + c];
+            p[k].set(v[0], v[1], v[2], v[3]);
+        }
+        return make(p, std::index_sequence_for<Particles...>{});
+    }
+
+    // Raw column k ({E,px,py,pz} per event) and the weight column.
+    double* column(size_t k) { return on_device ? fDevCols[k].p : fHostCols[k].data(); }
+    const double* column(size_t k) const { return on_device ? fDevCols[k].p : fHostCols[k].data(); }
+    double* weights() { return on_device ? fDevW.p : fHostW.data(); }
+
+    // Generation-time weights (what the reference's Generate computes and drops).
+    std::vector<double> GetWeights() const
+    {
+        std::vector<double> w(fN);
+        if (on_device && fN)
+            detail::throw_cuda(cudaMemcpy(w.data(), fDevW.p, fN * 8, cudaMemcpyDeviceToHost), "cudaMemcpy");
+        else if (fN)
+            w = fHostW;
+        return w;
+    }
+
+    // Events | Events.GetEventWeightFunctor(): PhaseSpaceWeight recomputed from the stored
+    // four-vectors (Decays.inl:215-231), evaluated eagerly.
+    std::vector<double> GetEventWeights() const
+    {
+        std::vector<double> w(fN);
+        if (!fN) return w;
+        with_device_columns([&](const double* const* cols) {
+            detail::DeviceBuffer<double> out(fN);
+            detail::throw_status(hps_event_weights(nparticles, fMasses, fMaxWeight, fN, cols, out.p, nullptr));
+            detail::throw_cuda(cudaMemcpy(w.data(), out.p, fN * 8, cudaMemcpyDeviceToHost), "cudaMemcpy");
+        });
+        return w;
+    }
+
+    // Decays::Unweight(seed) (Decays.inl:415-455): hit-or-miss on PhaseSpaceWeight/max weight;
+    // accepted events move to the front in their original order; returns how many.
+    size_t Unweight(size_t seed = 0x180ec6d33cfd0abaULL)
+    {
+        if (!fN) return 0;
+        if (on_device) {
+            // flags and the stable partition stay on the device (hps_unweight_compact)
+            const double* cols[nparticles];
+            double* outc[nparticles];
+            detail::DeviceBuffer<double> out[nparticles];
+            for (size_t k = 0; k < nparticles; ++k) {
+                cols[k] = fDevCols[k].p;
+                out[k].resize(4 * fN);
+                outc[k] = out[k].p;
+            }
+            detail::DeviceBuffer<uint8_t> f(fN);
+            detail::DeviceBuffer<double> wout(fN);
+            detail::DeviceBuffer<uint64_t> nacc(1);
+            detail::throw_status(hps_unweight_flags(nparticles, fMasses, fMaxWeight, fN, cols, seed, 0, f.p, nullptr));
+            detail::throw_status(hps_unweight_compact(nparticles, fN, cols, fDevW.p, f.p, outc, wout.p, nacc.p,
+                                                      nullptr, 0, nullptr));
+            uint64_t kept = 0;
+            detail::throw_cuda(cudaMemcpy(&kept, nacc.p, sizeof(kept), cudaMemcpyDeviceToHost), "cudaMemcpy");
+            for (size_t k = 0; k < nparticles; ++k) std::swap(fDevCols[k], out[k]);
+            std::swap(fDevW, wout);
+            return static_cast<size_t>(kept);
+        }
+        std::vector<uint8_t> flags(fN);
+        with_device_columns([&](const double* const* cols) {
+            detail::DeviceBuffer<uint8_t> f(fN);
+            detail::throw_status(hps_unweight_flags(nparticles, fMasses, fMaxWeight, fN, cols, seed, 0, f.p, nullptr));
+            detail::throw_cuda(cudaMemcpy(flags.data(), f.p, fN, cudaMemcpyDeviceToHost), "cudaMemcpy");
+        });
+        std::vector<size_t> order;
+        order.reserve(fN);
+        for (size_t i = 0; i < fN; ++i) if (flags[i]) order.push_back(i);
+        const size_t kept = order.size();
+        for (size_t i = 0; i < fN; ++i) if (!flags[i]) order.push_back(i);
+        permute(order);
+        return kept;
+    }
+
+private:
+    template <size_t... I>
+    static value_type make(const Vector4R (&p)[nparticles], std::index_sequence<I...>)
+    {
+        return value_type(Particles(p[I])...);
+    }
+
+    void init(size_t n)
+    {
+        double ecm = fMotherMass;
+        for (size_t i = 0; i < nparticles; ++i) ecm -= fMasses[i];
+        double emmax = ecm + fMasses[0], emmin = 0.0, wtmax = 1.0;
+        for (size_t i = 1; i < nparticles; ++i) {                 // Decays.h:100-118
+            emmin += fMasses[i - 1];
+            emmax += fMasses[i];
+            const double a = emmax, b = emmin, c = fMasses[i];
+            wtmax *= std::sqrt((a - b - c) * (a + b + c) * (a - b + c) * (a + b - c)) / (2 * a);
+        }
+        fMaxWeight = 1.0 / wtmax;
+        fN = n;
+        for (size_t k = 0; k < nparticles; ++k) {
+            if (on_device) fDevCols[k].resize(4 * n);
+            else fHostCols[k].assign(4 * n, 0.0);
+        }
+        if (on_device) fDevW.resize(n); else fHostW.assign(n, 0.0);
+    }
+
+    template <typename F> void with_device_columns(F&& f) const
+    {
+        const double* cols[nparticles];
+        if (on_device) {
+            for (size_t k = 0; k < nparticles; ++k) cols[k] = fDevCols[k].p;
+            f(cols);
+            return;
+        }
+        detail::DeviceBuffer<double> tmp[nparticles];
+        for (size_t k = 0; k < nparticles; ++k) {
+            tmp[k].resize(4 * fN);
+            detail::throw_cuda(cudaMemcpy(tmp[k].p, fHostCols[k].data(), fN * 32, cudaMemcpyHostToDevice), "cudaMemcpy");
+            cols[k] = tmp[k].p;
+        }
+        f(cols);
+    }
+
+    void permute(const std::vector<size_t>& order)
+    {
+        for (size_t k = 0; k <= nparticles; ++k) {
+            const size_t width = (k < nparticles) ? 4 : 1;
+            std::vector<double> src(fN * width), dst(fN * width);
+            double* col = (k < nparticles) ? column(k) : weights();
+            if (on_device)
+                detail::throw_cuda(cudaMemcpy(src.data(), col, fN * width * 8, cudaMemcpyDeviceToHost), "cudaMemcpy");
+            else
+                std::copy(col, col + fN * width, src.begin());
+            for (size_t i = 0; i < fN; ++i)
+                for (size_t c = 0; c < width; ++c) dst[i * width + c] = src[order[i] * width + c];
+            if (on_device)
+                detail::throw_cuda(cudaMemcpy(col, dst.data(), fN * width * 8, cudaMemcpyHostToDevice), "cudaMemcpy");
+            else
+                std::copy(dst.begin(), dst.end(), col);
+        }
+    }
+
+    double fMotherMass = 0.0;
+    double fMaxWeight = 0.0;
+    double fMasses[HPS_MAX_DAUGHTERS] = {};
+    size_t fN = 0;
+    detail::DeviceBuffer<double> fDevCols[nparticles];
+    detail::DeviceBuffer<double> fDevW;
+    std::vector<double> fHostCols[nparticles];
+    std::vector<double> fHostW;
+};
+
+// ------------------------------------------------------------------------------ multivector
+
+// Result columns of Evaluate: hydra::multivector<hydra::tuple<T...>, Backend> with one double
+// column per element (the first holds the weight).
+template <typename Tuple, typename Backend> class multivector;
+
+template <typename... T, typename Backend>
+class multivector<hydra::tuple<T...>, Backend> {
+public:
+    enum { ncols = sizeof...(T) };
+    static constexpr bool on_device = std::is_same<Backend, detail::DeviceBackend>::value;
+    explicit multivector(size_t n) : fN(n)
+    {
+        for (size_t k = 0; k < ncols; ++k) {
+            if (on_device) fDev[k].resize(n); else fHost[k].assign(n, 0.0);
+        }
+    }
+    size_t size() const { return fN; }
+    double* column(size_t k) { return on_device ? fDev[k].p : fHost[k].data(); }
+    std::vector<double> GetColumn(size_t k) const
+    {
+        std::vector<double> out(fN);
+        if (on_device && fN)
+            detail::throw_cuda(cudaMemcpy(out.data(), fDev[k].p, fN * 8, cudaMemcpyDeviceToHost), "cudaMemcpy");
+        else
+            out = fHost[k];
+        return out;
+    }
+
+private:
+    size_t fN;
+    detail::DeviceBuffer<double> fDev[ncols];
+    std::vector<double> fHost[ncols];
+};
+
+// ------------------------------------------------------------------------------ PhaseSpace
+
+template <size_t N, typename GRND = default_random_engine>
+class PhaseSpace {
+    static_assert(N >= 2 && N <= HPS_MAX_DAUGHTERS, "2..10 daughters");
+
+public:
+    PhaseSpace(double motherMass, const double (&daughtersMasses)[N]) { init(motherMass, daughtersMasses); }
+    PhaseSpace(double motherMass, std::array<GReal_t, N> const& daughtersMasses)
+    {
+        init(motherMass, daughtersMasses.data());
+    }
+    PhaseSpace(double motherMass, std::initializer_list<GReal_t> const& daughtersMasses)
+    {
+        if (daughtersMasses.size() < N) throw std::invalid_argument("[hydra::PhaseSpace]: too few masses");
+        init(motherMass, daughtersMasses.begin());
+    }
+
+    // Generate(mother, Decays) (PhaseSpace.inl:377-394): device Decays through hps_generate,
+    // host Decays through hps_generate_host.
+    template <typename... P, typename Backend>
+    void Generate(Vector4R const& mother, Decays<hydra::tuple<P...>, Backend>& events)
+    {
+        static_assert(sizeof...(P) == N, "Decays must hold N daughters");
+        hps_channel ch = channel(mother);
+        double* cols[N];
+        for (size_t k = 0; k < N; ++k) cols[k] = events.column(k);
+        if (Decays<hydra::tuple<P...>, Backend>::on_device) {
+            detail::throw_status(hps_generate(&ch, 0, events.size(), cols, events.weights(), nullptr, 0, fPrecision,
+                                              nullptr));
+            detail::throw_cuda(cudaStreamSynchronize(nullptr), "cudaStreamSynchronize");
+        } else {
+            detail::throw_status(hps_generate_host(&ch, 0, events.size(), cols, events.weights(), nullptr, 0,
+                                                   fPrecision, 0, nullptr));
+        }
+    }
+
+    // AverageOn(policy, mother, functor, n) (PhaseSpace.inl:255-273): (mean, sqrt(M2)/W).
+    template <typename Functor, typename Policy>
+    std::pair<GReal_t, GReal_t> AverageOn(Policy const&, Vector4R const& mother, Functor const& functor, size_t n)
+    {
+        static_assert(hps_fn::is_menu<Functor>::value,
+                      "AverageOn across the C ABI takes hydra::hps_fn::One, Mass2 or BW2");
+        hps_channel ch = channel(mother);
+        detail::DeviceBuffer<hps_stats> out(1);
+        detail::throw_status(hps_average_on(&ch, 0, n, &functor.f, out.p, nullptr, 0, fPrecision, nullptr));
+        hps_stats s;
+        detail::throw_cuda(cudaMemcpy(&s, out.p, sizeof(s), cudaMemcpyDeviceToHost), "cudaMemcpy");
+        return std::make_pair(s.mean, std::sqrt(s.m2) / s.w);
+    }
+
+    // Evaluate(mother, result, functors...) (PhaseSpace.inl:314-329): column 0 the weight,
+    // column k the k-th functor.
+    template <typename... T, typename Backend, typename... Functors>
+    void Evaluate(Vector4R const& mother, multivector<hydra::tuple<T...>, Backend>& result, Functors const&... fs)
+    {
+        static_assert(sizeof...(T) == sizeof...(Functors) + 1, "one result column per functor plus the weight");
+        const hps_functor menu[] = {fs.f...};
+        hps_channel ch = channel(mother);
+        const size_t n = result.size();
+        const bool dev = multivector<hydra::tuple<T...>, Backend>::on_device;
+        std::vector<detail::DeviceBuffer<double>> tmp;
+        double* out[sizeof...(Functors) + 1];
+        for (size_t k = 0; k <= sizeof...(Functors); ++k) {
+            if (dev) {
+                out[k] = result.column(k);
+            } else {
+                tmp.emplace_back(n);
+                out[k] = tmp.back().p;
+            }
+        }
+        detail::throw_status(hps_evaluate(&ch, 0, n, menu, sizeof...(Functors), out[0], out + 1, fPrecision, nullptr));
+        detail::throw_cuda(cudaStreamSynchronize(nullptr), "cudaStreamSynchronize");
+        if (!dev)
+            for (size_t k = 0; k <= sizeof...(Functors); ++k)
+                detail::throw_cuda(cudaMemcpy(result.column(k), out[k], n * 8, cudaMemcpyDeviceToHost), "cudaMemcpy");
+    }
+
+    GInt_t GetSeed() const { return static_cast<GInt_t>(fSeed); }
+    void SetSeed(GInt_t seed) { fSeed = static_cast<size_t>(static_cast<long long>(seed)); }
+    const GReal_t* GetMasses() const { return fMasses; }
+    double GetMaxWeight() const { return fMaxWeight; }
+    void SetMaxWeight(double w) { fMaxWeight = w; }
+    double GetMotherMass() const { return fMotherMass; }
+    void SetMotherMass(double m) { fMotherMass = m; }
+    double GetECM() const { return fECM; }
+    void SetECM(double e) { fECM = e; }
+    static double PDK(double a, double b, double c)
+    {
+        double x = (a - b - c) * (a + b + c) * (a - b + c) * (a + b - c);
+        x = std::sqrt(x) / (2 * a);
+        return x;
+    }
+
+    // Not in the reference: arithmetic of the kernels (HPS_PREC_FP64 default, HPS_PREC_FP32_FIX).
+    void SetPrecision(int32_t precision) { fPrecision = precision; }
+
+private:
+    void init(double motherMass, const double* masses)
+    {
+        hps_channel ch;
+        const double mother[4] = {motherMass, 0.0, 0.0, 0.0};
+        detail::throw_status(hps_channel_init(&ch, N, detail::engine_id<GRND>::value, 0, motherMass, masses, mother));
+        fMotherMass = motherMass;
+        for (size_t i = 0; i < N; ++i) fMasses[i] = masses[i];
+        fECM = ch.ecm;
+        fMaxWeight = ch.max_weight;
+        // default seed: 1 * (1 + hash_range(masses)) (PhaseSpace.inl:44,64)
+        fSeed = hps_default_seed(N, masses);
+    }
+
+    hps_channel channel(Vector4R const& mother) const
+    {
+        hps_channel ch;
+        detail::throw_status(hps_channel_init(&ch, N, detail::engine_id<GRND>::value, fSeed, fMotherMass, fMasses,
+                                              mother.data()));
+        ch.ecm = fECM;                // the values this object holds (SetECM / SetMaxWeight apply)
+        ch.max_weight = fMaxWeight;
+        return ch;
+    }
+
+    size_t fSeed = 1;
+    double fMotherMass = 0.0;
+    double fMaxWeight = 0.0;
+    double fECM = 0.0;
+    GReal_t fMasses[N] = {};
+    int32_t fPrecision = HPS_PREC_FP64;
+};
+
+}  // namespace hydra
+
+#endif  // HYDRA_HPS_PHASESPACE_HPP_

@@ -352,3 +352,18 @@ def test_generate_host_matches_device(api, torch, chunk):
     pf = torch.zeros((5, n, 4), dtype=torch.float64)
     api.generate_host(hch, 17, pf, None, None, chunk_events=chunk)
     assert np.array_equal(pf.numpy(), f)
+
+
+@pytest.mark.parametrize("n", [1, 4095, 4096, 100_003])
+def test_unweight_compact_is_stable_partition(api, torch, oracle, n):
+    hch = api.make_channel([K, PI, PI, PI, PI], 1.86484, 0x3039, 0)
+    four, w, fl = gpu_generate(api, torch, hch, 0, n, flags=True)
+    tf = torch.as_tensor(four, device="cuda")
+    tw = torch.as_tensor(w, device="cuda")
+    tfl = torch.as_tensor(fl, device="cuda")
+    out, wout, nacc = api.unweight_compact(tf, tfl, tw)
+    torch.cuda.synchronize()
+    order = np.concatenate([np.nonzero(fl)[0], np.nonzero(fl == 0)[0]])
+    assert int(nacc.item()) == int(fl.sum())
+    assert np.array_equal(out.cpu().numpy(), four[:, order])
+    assert np.array_equal(wout.cpu().numpy(), w[order])
