@@ -144,6 +144,10 @@ SIGNATURES = {
                               _sz, _i32, _vp]),
     "hps_average_on_noalloc": (_i32, [ctypes.POINTER(HpsChannel), _u64, _u64, ctypes.POINTER(HpsFunctor), _vp,
                                       _i32, _vp]),
+    "hps_generate_mothers": (_i32, [ctypes.POINTER(HpsChannel), _u64, _u64, _vp, _vp, _vp, _i32, _vp]),
+    "hps_average_on_mothers": (_i32, [ctypes.POINTER(HpsChannel), _u64, _u64, _vp, ctypes.POINTER(HpsFunctor), _vp,
+                                      _vp, _sz, _i32, _vp]),
+    "hps_evaluate_mothers": (_i32, [ctypes.POINTER(HpsChannel), _u64, _u64, _vp, _vp, _i32, _vp, _vp, _i32, _vp]),
     "hps_event_weights": (_i32, [_i32, _vp, _dbl, _u64, _vp, _vp, _vp]),
     "hps_unweight_flags": (_i32, [_i32, _vp, _dbl, _u64, _vp, _u64, _u64, _vp, _vp]),
     "hps_compact_workspace_size": (_sz, [_u64]),

@@ -170,6 +170,34 @@ def average_on(ch: HpsChannel, first: int, n: int, functor: HpsFunctor, out: tor
                                wbytes, _PRECISIONS[precision], _stream_handle(stream)))
 
 
+def generate_mothers(ch: HpsChannel, first: int, mothers: torch.Tensor, four: torch.Tensor, weights=None,
+                     precision="fp64", stream=None) -> None:
+    """DecayMothers: mothers [n, 4] (a Vector4R column), four [N, n, 4]."""
+    arr = _ptr_array([four[k] for k in range(four.shape[0])])
+    check(lib().hps_generate_mothers(ctypes.byref(ch), first, mothers.shape[0], _dptr(mothers),
+                                     ctypes.cast(arr, ctypes.c_void_p), _dptr(weights), _PRECISIONS[precision],
+                                     _stream_handle(stream)))
+
+
+def average_on_mothers(ch: HpsChannel, first: int, mothers: torch.Tensor, functor: HpsFunctor, out: torch.Tensor,
+                       precision="fp64", stream=None) -> None:
+    """AverageMothers; functor indices count the mother as particle 0."""
+    check(lib().hps_average_on_mothers(ctypes.byref(ch), first, mothers.shape[0], _dptr(mothers),
+                                       ctypes.byref(functor), _dptr(out), None, 0, _PRECISIONS[precision],
+                                       _stream_handle(stream)))
+
+
+def evaluate_mothers(ch: HpsChannel, first: int, mothers: torch.Tensor, functors: Sequence[HpsFunctor],
+                     weights: torch.Tensor | None, outs: Sequence[torch.Tensor], precision="fp64", stream=None):
+    """EvalMothers; functor indices count the mother as particle 0."""
+    fa = (HpsFunctor * max(1, len(functors)))(*functors)
+    arr = _ptr_array(outs)
+    check(lib().hps_evaluate_mothers(ctypes.byref(ch), first, mothers.shape[0], _dptr(mothers),
+                                     ctypes.cast(fa, ctypes.c_void_p), len(functors), _dptr(weights),
+                                     ctypes.cast(arr, ctypes.c_void_p), _PRECISIONS[precision],
+                                     _stream_handle(stream)))
+
+
 def event_weights(n_daughters: int, masses: Sequence[float], max_weight: float, four: torch.Tensor,
                   out: torch.Tensor, stream=None) -> None:
     n = four.shape[1]

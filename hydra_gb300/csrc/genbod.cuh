@@ -75,13 +75,16 @@ __device__ __forceinline__ double mass2(const double (&v)[4])
     return sub(sub(sub(mul(v[0], v[0]), mul(v[1], v[1])), mul(v[2], v[2])), mul(v[3], v[3]));
 }
 
-// One event.  p[k] = {E, px, py, pz} of daughter k.  Returns the generation-time weight.
+// The event body up to (not including) the final boost, from the stream (key, base), the
+// kinetic energy `ecm` and the initial weight factor `wt0`.  p[k] = {E, px, py, pz} of daughter
+// k.  Returns the generation-time weight wt0 * prod pdk.
 template <int N, int ENGINE>
-__device__ __forceinline__ double event(const DevChannel& ch, uint64_t evt, double (&p)[N][4])
+__device__ __forceinline__ double event_core(const DevChannel& ch, uint64_t key, uint64_t base, double ecm,
+                                             double wt0, double (&p)[N][4])
 {
     constexpr int NW = 3 * N - 4;
     uint64_t w[NW];
-    event_words<N, ENGINE>(ch.key, evt, w);
+    stream_words<N, ENGINE>(key, base, w);
     if constexpr (N > 3) sort_words<N - 2>(w);
 
     // invariant masses of the intermediate systems (DecayMother.h:170-197)
@@ -92,12 +95,12 @@ __device__ __forceinline__ double event(const DevChannel& ch, uint64_t evt, doub
         for (int n = 0; n < N; ++n) {
             const double rno = (n == 0) ? 0.0 : (n == N - 1) ? 1.0 : word_to_uniform<ENGINE>(w[n - 1]);
             sum = add(sum, ch.masses[n]);
-            invMas[n] = add(mul(rno, ch.ecm), sum);
+            invMas[n] = add(mul(rno, ecm), sum);
         }
     }
     // weight (DecayMother.h:203-212)
     double pd[N - 1];
-    double wt = ch.max_weight;
+    double wt = wt0;
 #pragma unroll
     for (int n = 0; n < N - 1; ++n) {
         pd[n] = pdk(invMas[n + 1], invMas[n], ch.masses[n + 1]);
@@ -143,11 +146,71 @@ __device__ __forceinline__ double event(const DevChannel& ch, uint64_t evt, doub
             }
         }
     }
-    // final boost to the mother's frame (DecayMother.h:264-269)
+    return wt;
+}
+
+// One event of DecayMother / AverageMother / EvalMother (DecayMother.h:163-277): the engine after
+// discard(evt + 3N), the constructor's ECM and max weight, final boost by the channel's beta
+// vector (DecayMother.h:264-269).
+template <int N, int ENGINE>
+__device__ __forceinline__ double event(const DevChannel& ch, uint64_t evt, double (&p)[N][4])
+{
+    const double wt = event_core<N, ENGINE>(ch, ch.key, evt + 3u * N, ch.ecm, ch.max_weight, p);
     if (ch.boost_active) {
 #pragma unroll
         for (int n = 0; n < N; ++n) boost_general(p[n], ch.beta[0], ch.beta[1], ch.beta[2]);
     }
+    return wt;
+}
+
+// Vector4R::applyBoostTo(Vector4R) (Vector4R.inl:236-248): boost by (px, py, pz) / E of mo.
+template <int N>
+__device__ __forceinline__ void boost_by_mother(double (&p)[N][4], const double (&mo)[4])
+{
+    const double bx = dvd(mo[1], mo[0]), by = dvd(mo[2], mo[0]), bz = dvd(mo[3], mo[0]);
+#pragma unroll
+    for (int n = 0; n < N; ++n) boost_general(p[n], bx, by, bz);
+}
+
+// DecayMothers / AverageMothers (DecayMothers.h:131-242): the same stream, ECM and weight as
+// `event`, final boost by the event's own mother.
+template <int N, int ENGINE>
+__device__ __forceinline__ double event_mother(const DevChannel& ch, uint64_t evt, const double (&mo)[4],
+                                               double (&p)[N][4])
+{
+    const double wt = event_core<N, ENGINE>(ch, ch.key, evt + 3u * N, ch.ecm, ch.max_weight, p);
+    boost_by_mother<N>(p, mo);
+    return wt;
+}
+
+// EvalMothers::hash, Szudzik pairing in size_t arithmetic (EvalMothers.h:131-140).
+__device__ __forceinline__ uint64_t szudzik(uint64_t a, uint64_t b)
+{
+    const uint64_t A = 2 * a, B = 2 * b;
+    return ((A >= B) ? A * A + A + B : A + B * B) / 2;
+}
+
+// EvalMothers (EvalMothers.h:143-283): engine seeded with hash(evt, seed) where evt passes
+// through GInt_t, no discard; ECM and maximum weight from the mother's own mass; final boost
+// by the mother.
+template <int N, int ENGINE>
+__device__ __forceinline__ double event_evalmothers(const DevChannel& ch, uint64_t evt, uint64_t seed,
+                                                    const double (&mo)[4], double (&p)[N][4])
+{
+    const int32_t ievt = static_cast<int32_t>(static_cast<uint32_t>(evt));
+    const uint64_t key = splitmix64(szudzik(static_cast<uint64_t>(static_cast<int64_t>(ievt)), seed));
+    double ecm = mass(mo);
+#pragma unroll
+    for (int n = 0; n < N; ++n) ecm = sub(ecm, ch.masses[n]);
+    double emmax = add(ecm, ch.masses[0]), emmin = 0.0, wtmax = 1.0;
+#pragma unroll
+    for (int n = 1; n < N; ++n) {
+        emmin = add(emmin, ch.masses[n - 1]);
+        emmax = add(emmax, ch.masses[n]);
+        wtmax = mul(wtmax, pdk(emmax, emmin, ch.masses[n]));
+    }
+    const double wt = event_core<N, ENGINE>(ch, key, 0, ecm, dvd(1.0, wtmax), p);
+    boost_by_mother<N>(p, mo);
     return wt;
 }
 

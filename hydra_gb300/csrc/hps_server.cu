@@ -82,6 +82,7 @@ struct hps_server {
     std::vector<int> free_slots;
     int allocs = 0;
     bool stop = false;
+    uint64_t wake_gen = 0;                 // bumped by submit / cancel / release / destroy
     hps_status fatal = HPS_OK;
     char fatal_msg[256] = "";
     std::thread thread;
@@ -293,10 +294,13 @@ void scheduler(hps_server* s)
             if (s->inflight.size() < 2 && !s->active.empty()) launched = launch(s);
         }
         if (launched) continue;
+        // Sleep until something can change: a launch completes, or a request is submitted,
+        // cancelled or released (a queued request blocked by the budget waits for a release).
+        // The timed wait also covers a completion whose notify raced this check.
         const uint64_t seen = s->completed.load(std::memory_order_acquire);
+        const uint64_t gen = s->wake_gen;
         s->cv_sched.wait_for(lock, std::chrono::microseconds(200), [&] {
-            return s->stop || s->completed.load(std::memory_order_acquire) != seen ||
-                   (s->fatal == HPS_OK && !s->pending.empty() && s->inflight.size() < 2);
+            return s->stop || s->completed.load(std::memory_order_acquire) != seen || s->wake_gen != gen;
         });
     }
 }
@@ -370,6 +374,7 @@ hps_status hps_server_submit(hps_server* s, const hps_request* req, hps_ticket* 
     s->pending.push_back(t);
     s->st.submitted++;
     *ticket = t;
+    s->wake_gen++;
     s->cv_sched.notify_all();
     return HPS_OK;
 }
@@ -422,7 +427,9 @@ hps_status hps_server_cancel(hps_server* s, hps_ticket t)
     r.t_done = now_s();
     s->st.cancelled++;
     s->finished.push_back(t);
+    s->wake_gen++;
     s->cv_done.notify_all();
+    s->cv_sched.notify_all();
     return HPS_OK;
 }
 
@@ -468,6 +475,7 @@ hps_status hps_server_release(hps_server* s, hps_ticket t)
     if (r.slot >= 0) s->free_slots.push_back(r.slot);
     s->reqs.erase(it);
     s->st.released++;
+    s->wake_gen++;
     s->cv_sched.notify_all();
     return HPS_OK;
 }
@@ -495,6 +503,7 @@ hps_status hps_server_destroy(hps_server* s)
             }
         }
         s->pending.clear();
+        s->wake_gen++;
         s->cv_sched.notify_all();
         s->cv_done.notify_all();
     }

@@ -58,12 +58,11 @@ __host__ __device__ __forceinline__ uint32_t squares3_word(uint64_t key, uint64_
 // Number of uniforms one event draws: N-2 invariant masses + 2(N-1) angles.
 template <int N> struct Draws { static constexpr int value = 3 * N - 4; };
 
-// All raw words of event `evt` (zero-extended for squares3).
+// All raw words a stream yields from counter state `base` (zero-extended for squares3).
 template <int N, int ENGINE>
-__device__ __forceinline__ void event_words(uint64_t key, uint64_t evt, uint64_t (&w)[3 * N - 4])
+__device__ __forceinline__ void stream_words(uint64_t key, uint64_t base, uint64_t (&w)[3 * N - 4])
 {
     constexpr int NW = 3 * N - 4;
-    const uint64_t base = evt + 3u * N;   // state after discard(evt + 3N), size_t arithmetic
     if constexpr (ENGINE == kPhilox) {
         constexpr int NB = (NW + 1) / 2;
 #pragma unroll
@@ -79,6 +78,13 @@ __device__ __forceinline__ void event_words(uint64_t key, uint64_t evt, uint64_t
 #pragma unroll
         for (int k = 0; k < NW; ++k) w[k] = squares3_word(key, base + k);
     }
+}
+
+// All raw words of event `evt`: the engine after discard(evt + 3N), size_t arithmetic.
+template <int N, int ENGINE>
+__device__ __forceinline__ void event_words(uint64_t key, uint64_t evt, uint64_t (&w)[3 * N - 4])
+{
+    stream_words<N, ENGINE>(key, evt + 3u * N, w);
 }
 
 template <int ENGINE>

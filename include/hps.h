@@ -191,6 +191,25 @@ hps_status hps_average_on_noalloc(const hps_channel* ch, uint64_t first_evt, uin
                                   const hps_functor* functor, hps_stats* out, int32_t precision,
                                   void* stream);
 
+/* Per-event mothers (FP64): mothers[n][4] is a device column of Vector4R, e.g. a daughter column
+ * of an earlier hps_generate for a decay chain (examples/phase_space/phsp_chain.inl:216-238).
+ *  hps_generate_mothers    Generate(mothers, daughters): DecayMothers (hydra/detail/functors/
+ *                          DecayMothers.h:131-260), the stream and ECM of hps_generate, each event
+ *                          boosted by its own mother.
+ *  hps_average_on_mothers  AverageOn(begin, end, functor): AverageMothers (AverageMothers.h:134-285).
+ *  hps_evaluate_mothers    Evaluate(mothers, result, functors): EvalMothers (EvalMothers.h:143-305):
+ *                          engine seeded with hash(evt, seed) without discard, ECM and maximum
+ *                          weight from each mother's mass.
+ * The functor sees (mother, daughter 0, ..., daughter N-1): its indices count the mother as 0. */
+hps_status hps_generate_mothers(const hps_channel* ch, uint64_t first_evt, uint64_t n, const double* mothers,
+                                double* const* cols, double* weights, int32_t precision, void* stream);
+hps_status hps_average_on_mothers(const hps_channel* ch, uint64_t first_evt, uint64_t n, const double* mothers,
+                                  const hps_functor* functor, hps_stats* out, void* workspace,
+                                  size_t workspace_bytes, int32_t precision, void* stream);
+hps_status hps_evaluate_mothers(const hps_channel* ch, uint64_t first_evt, uint64_t n, const double* mothers,
+                                const hps_functor* functors, int32_t n_functors, double* weights,
+                                double* const* out, int32_t precision, void* stream);
+
 /* PhaseSpaceWeight over stored events: replaces Events | Events.GetEventWeightFunctor()
  * (hydra/Decays.h:235-239, hydra/detail/Decays.inl:215-231).  out[n] = max_weight *
  * prod_i pdk(|R + p_i|, m_i, |R|). */

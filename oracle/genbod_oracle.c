@@ -189,13 +189,44 @@ static inline double mass2_of(const double v[4])
     return v[0] * v[0] - v[1] * v[1] - v[2] * v[2] - v[3] * v[3];
 }
 
-/* One GENBOD event; p is [N][4] (E, px, py, pz).  Returns the generation-time weight. */
-static double event_body(const hpso_channel* ch, uint64_t evt, double p[][4])
+/* Szudzik pairing of EvalMothers::hash (hydra/detail/functors/EvalMothers.h:131-140), size_t arithmetic. */
+static inline uint64_t szudzik(uint64_t a, uint64_t b)
+{
+    uint64_t A = 2 * a, B = 2 * b;
+    return ((A >= B) ? A * A + A + B : A + B * B) / 2;
+}
+
+/* One GENBOD event; p is [N][4] (E, px, py, pz).  Returns the generation-time weight.
+ * mode 0: DecayMother / AverageMother / EvalMother (DecayMother.h:163-277): engine seeded with
+ *         the channel seed after discard(evt+3N); final boost by the channel's beta vector.
+ * mode 1: DecayMothers / AverageMothers (DecayMothers.h:131-242): same stream and ECM, final boost
+ *         by the event's mother four-vector (applyBoostTo(Vector4R), Vector4R.inl:236-248).
+ * mode 2: EvalMothers (EvalMothers.h:143-283): engine seeded with hash((int)evt, seed) and no
+ *         discard; ECM and the maximum weight from the event mother's own mass; weight
+ *         (1/wtmax) * prod pdk; final boost by the mother. */
+static double event_body_ex(const hpso_channel* ch, uint64_t evt, double p[][4], int mode, const double* mother)
 {
     const int N = ch->n_daughters;
     const double* m = ch->masses;
     hpso_stream s;
-    stream_init(&s, ch->engine, ch->seed, evt + 3u * (uint64_t)N);
+    double ecm = ch->ecm;
+    double wt;
+    if (mode == 2) {
+        const int32_t ievt = (int32_t)(uint32_t)evt;               /* process(const GInt_t evt, ...) */
+        stream_init(&s, ch->engine, szudzik((uint64_t)(int64_t)ievt, ch->seed), 0);
+        ecm = mass_of(mother);
+        for (int n = 0; n < N; ++n) ecm -= m[n];
+        double emmax = ecm + m[0], emmin = 0.0, wtmax = 1.0;
+        for (int n = 1; n < N; ++n) {
+            emmin += m[n - 1];
+            emmax += m[n];
+            wtmax *= pdk(emmax, emmin, m[n]);
+        }
+        wt = 1.0 / wtmax;
+    } else {
+        stream_init(&s, ch->engine, ch->seed, evt + 3u * (uint64_t)N);
+        wt = ch->max_weight;
+    }
 
     double rno[HPSO_MAXN];
     rno[0] = 0.0;
@@ -215,10 +246,9 @@ static double event_body(const hpso_channel* ch, uint64_t evt, double p[][4])
     double invMas[HPSO_MAXN], sum = 0.0;
     for (int n = 0; n < N; ++n) {
         sum += m[n];
-        invMas[n] = rno[n] * ch->ecm + sum;
+        invMas[n] = rno[n] * ecm + sum;
     }
 
-    double wt = ch->max_weight;
     double pd[HPSO_MAXN] = {0};
     for (int n = 0; n < N - 1; ++n) {
         pd[n] = pdk(invMas[n + 1], invMas[n], m[n + 1]);
@@ -251,8 +281,19 @@ static double event_body(const hpso_channel* ch, uint64_t evt, double p[][4])
         double beta = pd[i] / sqrt(pd[i] * pd[i] + invMas[i] * invMas[i]);
         for (int j = 0; j <= i; ++j) boost(p[j], 0, beta, 0);
     }
-    for (int n = 0; n < N; ++n) boost(p[n], ch->beta[0], ch->beta[1], ch->beta[2]);
+    if (mode == 0) {
+        for (int n = 0; n < N; ++n) boost(p[n], ch->beta[0], ch->beta[1], ch->beta[2]);
+    } else {
+        const double e = mother[0];
+        const double bx = mother[1] / e, by = mother[2] / e, bz = mother[3] / e;
+        for (int n = 0; n < N; ++n) boost(p[n], bx, by, bz);
+    }
     return wt;
+}
+
+static double event_body(const hpso_channel* ch, uint64_t evt, double p[][4])
+{
+    return event_body_ex(ch, evt, p, 0, NULL);
 }
 
 static inline double functor_eval(const hpso_functor* f, double p[][4])
@@ -514,6 +555,70 @@ void hpso_store_step(const hpso_channel* ch, uint64_t first, uint64_t n, double*
             double u = (double)squares3_word(key, first + (uint64_t)e) / 4294967296.0;
             flags[e] = (wr / ch->max_weight > u) ? 1 : 0;
         }
+    }
+    (void)nthreads;
+}
+
+/* Generate / AverageOn / Evaluate over a range of mothers ([n][4] doubles, one per event).
+ * mode 1 (Generate, AverageOn) follows DecayMothers / AverageMothers, mode 2 (Evaluate) EvalMothers.
+ * The functor sees (mother, daughter 0, ..., daughter N-1) (AverageMothers.h:258-269,
+ * EvalMothers.h:295-302): its indices count the mother as particle 0. */
+void hpso_generate_mothers(const hpso_channel* ch, uint64_t first, uint64_t n, const double* mothers,
+                           double* out4, double* weights, int nthreads)
+{
+    const int N = ch->n_daughters;
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+#endif
+    for (int64_t e = 0; e < (int64_t)n; ++e) {
+        double p[HPSO_MAXN][4];
+        double w = event_body_ex(ch, first + (uint64_t)e, p, 1, mothers + 4 * e);
+        for (int k = 0; k < N; ++k)
+            memcpy(out4 + (((size_t)k * n + (size_t)e) * 4), p[k], 4 * sizeof(double));
+        if (weights) weights[e] = w;
+    }
+    (void)nthreads;
+}
+
+void hpso_average_mothers(const hpso_channel* ch, const hpso_functor* f, uint64_t first, uint64_t n,
+                          const double* mothers, double* out)
+{
+    hpso_stats total = {0.0, 0.0, 0.0};
+    for (uint64_t e = 0; e < n; ++e) {
+        double p[HPSO_MAXN][4];
+        hpso_stats y;
+        y.w = event_body_ex(ch, first + e, p, 1, mothers + 4 * e);
+        double pm[HPSO_MAXN + 1][4];                   /* (mother, daughters...) as the functor sees them */
+        memcpy(pm[0], mothers + 4 * e, sizeof(pm[0]));
+        memcpy(pm[1], p, sizeof(double) * 4 * (size_t)ch->n_daughters);
+        y.mean = functor_eval(f, pm);
+        y.m2 = 0.0;
+        total = stats_add(total, y);
+    }
+    out[0] = total.mean;
+    out[1] = total.m2;
+    out[2] = total.w;
+}
+
+void hpso_evaluate_mothers(const hpso_channel* ch, const hpso_functor* f, uint64_t first, uint64_t n,
+                           const double* mothers, double* out_w, double* out_f, double* out4, int nthreads)
+{
+    const int N = ch->n_daughters;
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+#endif
+    for (int64_t e = 0; e < (int64_t)n; ++e) {
+        double p[HPSO_MAXN][4];
+        out_w[e] = event_body_ex(ch, first + (uint64_t)e, p, 2, mothers + 4 * e);
+        double pm[HPSO_MAXN + 1][4];
+        memcpy(pm[0], mothers + 4 * e, sizeof(pm[0]));
+        memcpy(pm[1], p, sizeof(double) * 4 * (size_t)N);
+        out_f[e] = functor_eval(f, pm);
+        if (out4)
+            for (int k = 0; k < N; ++k)
+                memcpy(out4 + (((size_t)k * n + (size_t)e) * 4), p[k], 4 * sizeof(double));
     }
     (void)nthreads;
 }

@@ -86,9 +86,13 @@ def lib():
         L.hpso_average_on.argtypes = [P(Channel), P(Functor), u64, u64, vp, i32]
         L.hpso_store_step.argtypes = [P(Channel), u64, u64, vp, vp, u64, vp, i32]
         L.hpso_unweight_uniforms.argtypes = [u64, u64, u64, vp]
+        L.hpso_generate_mothers.argtypes = [P(Channel), u64, u64, vp, vp, vp, i32]
+        L.hpso_average_mothers.argtypes = [P(Channel), P(Functor), u64, u64, vp, vp]
+        L.hpso_evaluate_mothers.argtypes = [P(Channel), P(Functor), u64, u64, vp, vp, vp, vp, i32]
         L.hpso_max_threads.restype = i32
         for f in ("hpso_rng_words", "hpso_generate", "hpso_recompute_weights", "hpso_flags",
-                  "hpso_evaluate", "hpso_average_on", "hpso_store_step", "hpso_unweight_uniforms"):
+                  "hpso_evaluate", "hpso_average_on", "hpso_store_step", "hpso_unweight_uniforms",
+                  "hpso_generate_mothers", "hpso_average_mothers", "hpso_evaluate_mothers"):
             getattr(L, f).restype = None
         _lib = L
     return _lib
@@ -185,6 +189,36 @@ def store_step(ch: Channel, first: int, n: int, useed: int, four=None, w=None, f
     lib().hpso_store_step(ctypes.byref(ch), first, n, _ptr(four), _ptr(w), useed, _ptr(fl),
                           nthreads)
     return four, w, fl
+
+
+def generate_mothers(ch: Channel, first: int, mothers: np.ndarray, nthreads: int = 0):
+    """DecayMothers: (four [N, n, 4], weights [n]) for mothers [n, 4]."""
+    mothers = np.ascontiguousarray(mothers, dtype=np.float64)
+    n = mothers.shape[0]
+    four = np.zeros((ch.n_daughters, n, 4), dtype=np.float64)
+    w = np.zeros(n, dtype=np.float64)
+    lib().hpso_generate_mothers(ctypes.byref(ch), first, n, _ptr(mothers), _ptr(four), _ptr(w), nthreads)
+    return four, w
+
+
+def average_mothers(ch: Channel, fn: Functor, first: int, mothers: np.ndarray):
+    """AverageMothers, sequential fold: (mean, M2, W).  Functor indices: 0 = mother."""
+    mothers = np.ascontiguousarray(mothers, dtype=np.float64)
+    out = np.zeros(3, dtype=np.float64)
+    lib().hpso_average_mothers(ctypes.byref(ch), ctypes.byref(fn), first, mothers.shape[0], _ptr(mothers), _ptr(out))
+    return float(out[0]), float(out[1]), float(out[2])
+
+
+def evaluate_mothers(ch: Channel, fn: Functor, first: int, mothers: np.ndarray, nthreads: int = 0):
+    """EvalMothers: (weights [n], functor values [n], four [N, n, 4]).  Functor indices: 0 = mother."""
+    mothers = np.ascontiguousarray(mothers, dtype=np.float64)
+    n = mothers.shape[0]
+    w = np.zeros(n)
+    f = np.zeros(n)
+    four = np.zeros((ch.n_daughters, n, 4))
+    lib().hpso_evaluate_mothers(ctypes.byref(ch), ctypes.byref(fn), first, n, _ptr(mothers), _ptr(w), _ptr(f),
+                                _ptr(four), nthreads)
+    return w, f, four
 
 
 def max_threads() -> int:

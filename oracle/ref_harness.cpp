@@ -22,6 +22,7 @@
  *   ref_harness gen  N engine seed n M m0..m{N-1} fsel fi fj fa fb useed mx my mz out.bin
  *   ref_harness avg  N engine seed n M m0..m{N-1} fsel fi fj fa fb out.bin
  *   ref_harness time N engine seed n M m0..m{N-1} fsel fi fj fa fb reps
+ *   ref_harness mothers N engine seed n M m0..m{N-1} fsel fi fj fa fb out.bin
  * engine: 0 = hydra::philox (Philox2x64, 7 rounds), 1 = hydra::default_random_engine (squares3)
  * fsel:   0 = constant 1, 1 = mass2(p_i+p_j), 2 = 1/((a^2 - mass2(p_i+p_j))^2 + (a*b)^2)
  * seed:   gen/avg/time: passed to PhaseSpace::SetSeed(GInt_t), -1 keeps the default (hash) seed;
@@ -34,6 +35,8 @@
 #include <hydra/Lambda.h>
 #include <hydra/Tuple.h>
 #include <hydra/multivector.h>
+#include <hydra/Range.h>
+#include <hydra/Placeholders.h>
 #include <hydra/host/System.h>
 #include <hydra/device/System.h>
 #include <hydra/detail/random/EngineR123.h>
@@ -101,6 +104,7 @@ inline double fmenu(FSpec const& f, hydra::Vector4R const* p)
 #define LAM_ARGS_8  LAM_ARGS_7, HV p7
 #define LAM_ARGS_9  LAM_ARGS_8, HV p8
 #define LAM_ARGS_10 LAM_ARGS_9, HV p9
+#define LAM_ARGS_11 LAM_ARGS_10, HV p10
 #define LAM_NAMES_2  p0, p1
 #define LAM_NAMES_3  LAM_NAMES_2, p2
 #define LAM_NAMES_4  LAM_NAMES_3, p3
@@ -110,6 +114,7 @@ inline double fmenu(FSpec const& f, hydra::Vector4R const* p)
 #define LAM_NAMES_8  LAM_NAMES_7, p7
 #define LAM_NAMES_9  LAM_NAMES_8, p8
 #define LAM_NAMES_10 LAM_NAMES_9, p9
+#define LAM_NAMES_11 LAM_NAMES_10, p10
 
 template <size_t N> struct menu_lambda;
 #define MENU_LAMBDA(NN)                                                        \
@@ -122,7 +127,7 @@ template <size_t N> struct menu_lambda;
         }                                                                      \
     };
 MENU_LAMBDA(2) MENU_LAMBDA(3) MENU_LAMBDA(4) MENU_LAMBDA(5) MENU_LAMBDA(6)
-MENU_LAMBDA(7) MENU_LAMBDA(8) MENU_LAMBDA(9) MENU_LAMBDA(10)
+MENU_LAMBDA(7) MENU_LAMBDA(8) MENU_LAMBDA(9) MENU_LAMBDA(10) MENU_LAMBDA(11)
 
 template <typename T>
 void write_bin(const char* path, std::vector<T> const& v)
@@ -261,6 +266,61 @@ void run_time(Args const& a)
                 a.n, N, best_gen, best_avg);
 }
 
+// Per-event mothers for the *Mothers variants: mass M(1 + 0.05 sin(0.7 i)), momentum
+// (0.3 sin(0.1 i), -0.7 cos(0.37 i), 1.1 sin(0.23 i + 1)) GeV, on shell.
+std::vector<hydra::Vector4R> make_mothers(double M, size_t n)
+{
+    std::vector<hydra::Vector4R> v(n);
+    for (size_t i = 0; i < n; ++i) {
+        const double mi = M * (1.0 + 0.05 * std::sin(0.7 * i));
+        const double px = 0.3 * std::sin(0.1 * i), py = -0.7 * std::cos(0.37 * i), pz = 1.1 * std::sin(0.23 * i + 1.0);
+        v[i] = hydra::Vector4R(std::sqrt(mi * mi + px * px + py * py + pz * pz), px, py, pz);
+    }
+    return v;
+}
+
+// Generate(mothers, daughters) (DecayMothers), AverageOn(begin, end, functor) (AverageMothers) and
+// Evaluate(mothers, result, functor) (EvalMothers).
+// layout: [n*4 mothers][n*N*4 Generate four-vectors][n Evaluate weights][n Evaluate functor values]
+//         [mean, err of AverageOn]
+template <size_t N, typename GRND>
+void run_mothers(Args const& a)
+{
+    typedef typename ptypes<N>::type PT;
+    auto phsp = make_phsp<N, GRND>(a);
+    double masses[N];
+    for (size_t i = 0; i < N; ++i) masses[i] = a.m[i];
+    auto mothers_v = make_mothers(a.M, a.n);
+    hydra::multivector<hydra::tuple<D0>, hydra::host::sys_t> mothers(a.n);
+    for (size_t i = 0; i < a.n; ++i) hydra::get<0>(mothers[i]) = mothers_v[i];
+    hydra::Decays<PT, hydra::host::sys_t> events(a.M, masses, a.n);
+    auto mbegin = mothers.begin(hydra::placeholders::_0);
+    auto mend = mothers.end(hydra::placeholders::_0);
+    phsp.Generate(mbegin, mend, events.begin());
+    // AverageMothers / EvalMothers hand the functor (mother, daughter 0, ..., daughter N-1)
+    auto functor = menu_lambda<N + 1>::make(a.f);
+    hydra::multivector<hydra::tuple<WCol, FCol>, hydra::host::sys_t> evals(a.n);
+    // the range overload (PhaseSpace.inl:331-348); the iterator overload (:302-309) passes
+    // fMotherMass to EvalMothers' constructor and does not compile
+    phsp.Evaluate(hydra::make_range(mbegin, mend), evals, functor);
+    auto avg = phsp.AverageOn(mbegin, mend, functor);
+    std::vector<double> out;
+    for (size_t i = 0; i < a.n; ++i)
+        for (int c = 0; c < 4; ++c) out.push_back(mothers_v[i].get(c));
+    for (size_t i = 0; i < a.n; ++i) {
+        auto ev = events[i];
+        hydra::Vector4R p[N];
+        hydra::detail::assignTupleToArray(ev, p);
+        for (size_t k = 0; k < N; ++k)
+            for (int c = 0; c < 4; ++c) out.push_back(p[k].get(c));
+    }
+    for (size_t i = 0; i < a.n; ++i) out.push_back(hydra::get<0>(evals[i]));
+    for (size_t i = 0; i < a.n; ++i) out.push_back(hydra::get<1>(evals[i]));
+    out.push_back(avg.first);
+    out.push_back(avg.second);
+    write_bin(a.out, out);
+}
+
 template <size_t N, typename GRND>
 void dispatch_mode(Args const& a)
 {
@@ -268,6 +328,7 @@ void dispatch_mode(Args const& a)
     else if (a.mode == "gen") run_gen<N, GRND>(a);
     else if (a.mode == "avg") run_avg<N, GRND>(a);
     else if (a.mode == "time") run_time<N, GRND>(a);
+    else if (a.mode == "mothers") run_mothers<N, GRND>(a);
     else { std::fprintf(stderr, "unknown mode %s\n", a.mode.c_str()); std::exit(2); }
 }
 

@@ -55,6 +55,14 @@ AVG_CASES = [
 ]
 
 
+# (name, N, engine, seed, n, M, masses, functor over (mother, daughters...))
+MOTHER_CASES = [
+    ("mothers_n3_philox", 3, 0, 12345, 96, 5.27934, [3.0969, K, PI], (1, 0, 2, 0.0, 0.0)),
+    ("mothers_n5_squares3", 5, 1, 777, 64, 1.86484, [K, PI, PI, PI, PI], (2, 1, 2, 0.8955, 0.0473)),
+    ("mothers_n2_philox", 2, 0, 3, 64, 3.0969, [0.10566, 0.10566], (1, 1, 2, 0.0, 0.0)),
+]
+
+
 def run(args, out):
     subprocess.run([str(REF)] + [str(a) for a in args] + [str(out)], check=True)
     return out
@@ -93,6 +101,18 @@ def main():
         d = np.fromfile(run(args, tmp), dtype=np.float64)
         fixtures[name] = dict(N=N, engine=eng, seed=seed, n=n, M=M, masses=np.array(m),
                               functor=np.array(f), mean=d[0], err=d[1])
+    for name, N, eng, seed, n, M, m, f in MOTHER_CASES:
+        args = ["mothers", N, eng, seed, n, fnum(M)] + [fnum(x) for x in m] + \
+               [f[0], f[1], f[2], fnum(f[3]), fnum(f[4])]
+        d = np.fromfile(run(args, tmp), dtype=np.float64)
+        o = n * 4
+        fx = dict(N=N, engine=eng, seed=seed, n=n, M=M, masses=np.array(m), functor=np.array(f),
+                  mothers=d[:o].reshape(n, 4))
+        fx["four"] = d[o:o + n * N * 4].reshape(n, N, 4).transpose(1, 0, 2).copy()
+        o += n * N * 4
+        fx["eval_w"], fx["eval_f"] = d[o:o + n], d[o + n:o + 2 * n]
+        fx["avg_mean"], fx["avg_err"] = d[o + 2 * n], d[o + 2 * n + 1]
+        fixtures[name] = fx
     tmp.unlink()
     for name, fx in fixtures.items():
         np.savez_compressed(HERE / f"{name}.npz", **fx)

@@ -13,7 +13,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from conftest import AVG_GOLDEN, GEN_GOLDEN, REPO, RNG_GOLDEN, load_golden
+from conftest import AVG_GOLDEN, GEN_GOLDEN, MOTHER_GOLDEN, REPO, RNG_GOLDEN, load_golden
 
 REF = REPO / "oracle" / "_ref" / "ref_harness_cpp"
 
@@ -134,3 +134,19 @@ def test_oracle_against_live_reference(oracle, tmp_path, N, engine, seed):
     four, w = oracle.generate(ch, 0, n, nthreads=1)
     assert np.array_equal(four, d[:n * N * 4].reshape(n, N, 4).transpose(1, 0, 2))
     assert np.array_equal(w, d[n * N * 4:n * N * 4 + n])
+
+
+@pytest.mark.parametrize("name", MOTHER_GOLDEN)
+def test_mothers_variants_bit_exact(oracle, name):
+    """DecayMothers (Generate), AverageMothers (AverageOn, sequential fold) and EvalMothers
+    (Evaluate: hash(evt, seed) streams, per-event ECM from the mother's mass)."""
+    g = load_golden(name)
+    ch = oracle.make_channel(g["masses"], float(g["M"]), int(g["seed"]), int(g["engine"]))
+    four, _ = oracle.generate_mothers(ch, 0, g["mothers"], nthreads=1)
+    assert np.array_equal(four, g["four"])
+    f = g["functor"]
+    fn = oracle.make_functor(int(f[0]), int(f[1]), int(f[2]), float(f[3]), float(f[4]))
+    w, fv, _ = oracle.evaluate_mothers(ch, fn, 0, g["mothers"], nthreads=1)
+    assert np.array_equal(w, g["eval_w"]) and np.array_equal(fv, g["eval_f"])
+    mean, m2, W = oracle.average_mothers(ch, fn, 0, g["mothers"])
+    assert mean == g["avg_mean"] and np.sqrt(m2) / W == g["avg_err"]
