@@ -24,10 +24,12 @@ HPS_MAX_DAUGHTERS = 10
 HPS_AVG_TILE = 4096
 
 OK, ERR_BAD_ARG, ERR_NO_ENERGY, ERR_OOM, ERR_BUDGET, ERR_TIMEOUT, ERR_CUDA, ERR_UNSUPPORTED = range(8)
-ENGINE_PHILOX, ENGINE_SQUARES3 = 0, 1
+ENGINE_PHILOX, ENGINE_SQUARES3, ENGINE_MINSTD = 0, 1, 2
 PREC_FP64, PREC_FP32_FIX = 0, 1
 FN_ONE, FN_MASS2, FN_BW2 = 0, 1, 2
 DEFAULT_UNWEIGHT_SEED = 0x180EC6D33CFD0ABA   # hydra/Decays.h:253
+DEFAULT_FUNCTOR_UNWEIGHT_SEED = 0x39ABDC4529B1661C   # hydra/Decays.h:261
+HIST_UNIT, HIST_COLUMN, HIST_PHSP_WEIGHT = 0, 1, 2
 
 
 class HpsChannel(ctypes.Structure):
@@ -50,6 +52,16 @@ class HpsFunctor(ctypes.Structure):
         ("reserved", ctypes.c_int32),
         ("a", ctypes.c_double),
         ("b", ctypes.c_double),
+    ]
+
+
+class HpsHist2D(ctypes.Structure):
+    _fields_ = [
+        ("pair_a", ctypes.c_int32 * 2),
+        ("pair_b", ctypes.c_int32 * 2),
+        ("grid", ctypes.c_uint64 * 2),
+        ("lower", ctypes.c_double * 2),
+        ("upper", ctypes.c_double * 2),
     ]
 
 
@@ -153,6 +165,13 @@ SIGNATURES = {
     "hps_compact_workspace_size": (_sz, [_u64]),
     "hps_unweight_compact": (_i32, [_i32, _u64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "hps_rng_words": (_i32, [_i32, _i32, _u64, _u64, _u64, _vp, _vp]),
+    "hps_reweight": (_i32, [_i32, _vp, _dbl, ctypes.POINTER(HpsFunctor), _u64, _vp, _vp, _vp, _vp]),
+    "hps_weight_flags": (_i32, [_u64, _vp, _dbl, _vp, _u64, _u64, _vp, _vp]),
+    "hps_dalitz_histogram": (_i32, [_i32, _vp, _dbl, _u64, _vp, _vp, _i32, ctypes.POINTER(HpsHist2D), _vp, _vp]),
+    "hps_generate_dalitz": (_i32, [ctypes.POINTER(HpsChannel), _u64, _u64, _i32, ctypes.POINTER(HpsHist2D), _vp,
+                                   _vp]),
+    "hps_range_channel": (_i32, [ctypes.POINTER(HpsChannel), _i32, _vp, _vp, _u64]),
+    "hps_generate_range": (_i32, [ctypes.POINTER(HpsChannel), _u64, _u64, _vp, _vp, _vp]),
     "hps_default_seed": (_u64, [_i32, _vp]),
     "hps_batch_create": (_i32, [_vp, _i32, _u64, _i32, _vp]),
     "hps_batch_set_items": (_i32, [_vp, _vp, _i32, _vp]),

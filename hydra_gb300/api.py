@@ -22,6 +22,7 @@ import torch
 from . import (
     MODE_AVERAGE, MODE_STORE, HpsBatchItem, HpsBatchTuning, HpsRequest, HpsResult, HpsServerConfig,
     HpsServerStats,
+    DEFAULT_FUNCTOR_UNWEIGHT_SEED, HIST_COLUMN, HIST_PHSP_WEIGHT, HIST_UNIT, HpsHist2D,
     DEFAULT_UNWEIGHT_SEED, ENGINE_PHILOX, ENGINE_SQUARES3, ERR_BAD_ARG, ERR_NO_ENERGY, ERR_TIMEOUT, FN_BW2, FN_MASS2, FN_ONE,
     HPS_MAX_DAUGHTERS, PREC_FP32_FIX, PREC_FP64, HpsChannel, HpsError, HpsFunctor, check, lib,
 )
@@ -232,6 +233,74 @@ def unweight_compact(four: torch.Tensor, flags: torch.Tensor, weights: torch.Ten
                                      ctypes.cast(cout, ctypes.c_void_p), _dptr(wout), _dptr(nacc), None, 0,
                                      _stream_handle(stream)))
     return out, wout, nacc
+
+
+def reweight(n_daughters: int, masses: Sequence[float], max_weight: float, functor: HpsFunctor,
+             four: torch.Tensor, out: torch.Tensor | None, max_out: torch.Tensor | None = None, stream=None) -> None:
+    """PhaseSpaceReweight over stored events: out[e] = PhaseSpaceWeight * functor; max_out (a
+    1-element float64 CUDA tensor) receives the largest value."""
+    n = four.shape[1]
+    arr = _ptr_array([four[k] for k in range(n_daughters)])
+    m = _double_array(masses)
+    check(lib().hps_reweight(n_daughters, ctypes.cast(m, ctypes.c_void_p), max_weight, ctypes.byref(functor), n,
+                             ctypes.cast(arr, ctypes.c_void_p), _dptr(out), _dptr(max_out), _stream_handle(stream)))
+
+
+def weight_flags(weights: torch.Tensor, flags: torch.Tensor, max_weight: float | torch.Tensor,
+                 unweight_seed: int = DEFAULT_FUNCTOR_UNWEIGHT_SEED, first: int = 0, stream=None) -> None:
+    """flags[e] = weights[e] / W > u(first + e); W a float or a 1-element CUDA tensor."""
+    dev = max_weight if isinstance(max_weight, torch.Tensor) else None
+    host = 0.0 if dev is not None else float(max_weight)
+    check(lib().hps_weight_flags(weights.shape[0], _dptr(weights), host, _dptr(dev), unweight_seed & (2**64 - 1),
+                                 first, _dptr(flags), _stream_handle(stream)))
+
+
+def hist2d(pair_a=(0, 1), pair_b=(1, 2), grid=(100, 100), lower=(0.0, 0.0), upper=(1.0, 1.0)) -> HpsHist2D:
+    h = HpsHist2D()
+    h.pair_a[0], h.pair_a[1] = pair_a
+    h.pair_b[0], h.pair_b[1] = pair_b
+    h.grid[0], h.grid[1] = (int(g) for g in grid)
+    h.lower[0], h.lower[1] = (float(x) for x in lower)
+    h.upper[0], h.upper[1] = (float(x) for x in upper)
+    return h
+
+
+_HIST_WEIGHTS = {"unit": HIST_UNIT, "column": HIST_COLUMN, "phsp": HIST_PHSP_WEIGHT,
+                 HIST_UNIT: HIST_UNIT, HIST_COLUMN: HIST_COLUMN, HIST_PHSP_WEIGHT: HIST_PHSP_WEIGHT}
+
+
+def dalitz_histogram(n_daughters: int, masses: Sequence[float], max_weight: float, four: torch.Tensor,
+                     hist: HpsHist2D, bins: torch.Tensor, weights: torch.Tensor | None = None, weight_mode="phsp",
+                     stream=None) -> None:
+    n = four.shape[1]
+    arr = _ptr_array([four[k] for k in range(n_daughters)])
+    m = _double_array(masses)
+    check(lib().hps_dalitz_histogram(n_daughters, ctypes.cast(m, ctypes.c_void_p), max_weight, n,
+                                     ctypes.cast(arr, ctypes.c_void_p), _dptr(weights), _HIST_WEIGHTS[weight_mode],
+                                     ctypes.byref(hist), _dptr(bins), _stream_handle(stream)))
+
+
+def generate_dalitz(ch: HpsChannel, first: int, n: int, hist: HpsHist2D, bins: torch.Tensor, weight_mode="phsp",
+                    stream=None) -> None:
+    check(lib().hps_generate_dalitz(ctypes.byref(ch), first, n, _HIST_WEIGHTS[weight_mode], ctypes.byref(hist),
+                                    _dptr(bins), _stream_handle(stream)))
+
+
+def range_channel(masses: Sequence[float], mother: Sequence[float], seed: int) -> HpsChannel:
+    ch = HpsChannel()
+    m = _double_array(masses)
+    mo = _double_array(list(mother))
+    check(lib().hps_range_channel(ctypes.byref(ch), len(masses), ctypes.cast(m, ctypes.c_void_p),
+                                  ctypes.cast(mo, ctypes.c_void_p), int(seed) & (2**64 - 1)))
+    return ch
+
+
+def generate_range(ch: HpsChannel, first: int, four: torch.Tensor, weights: torch.Tensor | None = None,
+                   stream=None) -> None:
+    N, n = four.shape[0], four.shape[1]
+    arr = _ptr_array([four[k] for k in range(N)])
+    check(lib().hps_generate_range(ctypes.byref(ch), first, n, ctypes.cast(arr, ctypes.c_void_p), _dptr(weights),
+                                   _stream_handle(stream)))
 
 
 def rng_words(n_daughters: int, engine, seed: int, first: int, n: int, out: torch.Tensor, stream=None) -> None:
@@ -499,6 +568,50 @@ class Decays:
             self.weights = w
         return int(nacc.item())
 
+    def GetEventReweights(self, functor: HpsFunctor, stream=None) -> torch.Tensor:
+        """Events | Events.GetEventWeightFunctor(functor) (Decays.h:243-250), evaluated eagerly."""
+        out = torch.empty(len(self), dtype=torch.float64, device=self.four.device)
+        reweight(len(self.masses), self.masses, self.max_weight, functor, self.four, out, None, stream)
+        return out
+
+    def UnweightFunctor(self, functor: HpsFunctor, weight: float = -1.0,
+                        seed: int = DEFAULT_FUNCTOR_UNWEIGHT_SEED) -> int:
+        """Decays::Unweight(functor, weight, seed) (Decays.inl:458-511): hit-or-miss on
+        PhaseSpaceWeight * functor against weight, or against the largest such value when weight
+        <= 0; accepted events stable-partitioned to the front; returns their count."""
+        n = len(self)
+        rw = torch.empty(n, dtype=torch.float64, device=self.four.device)
+        mx = torch.empty(1, dtype=torch.float64, device=self.four.device)
+        reweight(len(self.masses), self.masses, self.max_weight, functor, self.four, rw, mx)
+        flags = torch.empty(n, dtype=torch.uint8, device=self.four.device)
+        weight_flags(rw, flags, mx if weight <= 0.0 else float(weight), seed, 0)
+        self.four, w, nacc = unweight_compact(self.four, flags, self.weights)
+        if self.weights is not None:
+            self.weights = w
+        return int(nacc.item())
+
+    def DalitzHistogram(self, grid=(100, 100), lower=(0.0, 0.0), upper=(1.0, 1.0), pair_a=(0, 1), pair_b=(1, 2),
+                        weight_mode="phsp") -> torch.Tensor:
+        """make_dense_histogram<double,2>(..., Events | dalitz, Events | GetEventWeightFunctor())
+        as in the reference's phsp_basic example: grid0*grid1 bins then underflow, overflow."""
+        bins = torch.empty(int(grid[0]) * int(grid[1]) + 2, dtype=torch.float64, device=self.four.device)
+        dalitz_histogram(len(self.masses), self.masses, self.max_weight, self.four,
+                         hist2d(pair_a, pair_b, grid, lower, upper), bins, self.weights, weight_mode)
+        torch.cuda.current_stream().synchronize()
+        return bins
+
+
+def phase_space_range(mother, masses: Sequence[float], seed: int, length: int, first: int = 0):
+    """phase_space_range(mother, masses, seed, length) (PhaseSpaceRange.inl:46-73), materialised:
+    returns (weights [length], four [N, length, 4]) of events first .. first+length-1."""
+    mom = mother.as_list() if isinstance(mother, Vector4R) else list(mother)
+    ch = range_channel(masses, mom, seed)
+    four = torch.empty((len(masses), length, 4), dtype=torch.float64, device="cuda")
+    w = torch.empty(length, dtype=torch.float64, device="cuda")
+    generate_range(ch, first, four, w)
+    torch.cuda.current_stream().synchronize()
+    return w, four
+
 
 class PhaseSpace:
     """hydra::PhaseSpace<N, GRND> (hydra/PhaseSpace.h:86-346)."""
@@ -565,3 +678,35 @@ class PhaseSpace:
                  self.precision)
         torch.cuda.current_stream().synchronize()
         return res
+
+    def DalitzHistogram(self, mother, n: int, grid=(100, 100), lower=(0.0, 0.0), upper=(1.0, 1.0), pair_a=(0, 1),
+                        pair_b=(1, 2), weight_mode="phsp") -> torch.Tensor:
+        """Generate + Dalitz histogram fused: the events are binned where they are made and
+        never stored (FP64; weight_mode "phsp" uses the generation-time weight)."""
+        bins = torch.empty(int(grid[0]) * int(grid[1]) + 2, dtype=torch.float64, device="cuda")
+        generate_dalitz(self._channel(mother), 0, n, hist2d(pair_a, pair_b, grid, lower, upper), bins, weight_mode)
+        torch.cuda.current_stream().synchronize()
+        return bins
+
+
+class PhaseSpaceIntegrator:
+    """hydra::PhaseSpaceIntegrator<N, Backend, GRND> (hydra/PhaseSpaceIntegrator.h:52-160):
+    Integrate(functor) is AverageOn(mother at rest, functor, n) of a PhaseSpace with the
+    default seed (PhaseSpaceIntegrator.inl:37-42)."""
+
+    def __init__(self, mother_mass: float, masses: Sequence[float], n: int, engine="default", precision="fp64"):
+        self.generator = PhaseSpace(mother_mass, masses, engine, precision)
+        self.mother = Vector4R(float(mother_mass), 0.0, 0.0, 0.0)
+        self.n_samples = int(n)
+
+    def GetGenerator(self) -> PhaseSpace:
+        return self.generator
+
+    def GetMother(self) -> Vector4R:
+        return self.mother
+
+    def GetNSamples(self) -> int:
+        return self.n_samples
+
+    def Integrate(self, functor: HpsFunctor):
+        return self.generator.AverageOn(self.mother, functor, self.n_samples)

@@ -36,6 +36,24 @@ hps_status launch_average(const hps_channel* channel, const DevChannel& ch, cons
                           uint64_t first_evt, uint64_t n, hps_stats* out, hps_stats* partials,
                           int32_t precision, cudaStream_t stream);
 
+// Stored events: N daughter columns of Vector4R (32 bytes per event, 16-byte aligned).
+struct ConstCols { const double* p[HPS_MAX_DAUGHTERS]; };
+
+template <int N>
+__device__ __forceinline__ void load_event(const ConstCols& cols, uint64_t e, double (&p)[N][4])
+{
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        const double2 a = __ldg(reinterpret_cast<const double2*>(cols.p[k] + 4 * e));
+        const double2 b = __ldg(reinterpret_cast<const double2*>(cols.p[k] + 4 * e) + 1);
+        p[k][0] = a.x; p[k][1] = a.y; p[k][2] = b.x; p[k][3] = b.y;
+    }
+}
+
+// Validates (n_daughters, masses, cols) of a stored sample; ch gets the masses and max_weight.
+hps_status stored_event_args(int32_t n_daughters, const double* masses, uint64_t n, const double* const* cols,
+                             ConstCols* cc, DevChannel* ch, double max_weight);
+
 // Events [first, first + n) must not run past index 2^64 - 1.
 inline bool range_ok(uint64_t first, uint64_t n) { return n == 0 || first + (n - 1) >= first; }
 

@@ -29,6 +29,8 @@ hps_status to_device_channel(const hps_channel* ch, DevChannel* out)
     if (!ch) return set_error(HPS_ERR_BAD_ARG, "channel is NULL");
     if (ch->n_daughters < 2 || ch->n_daughters > HPS_MAX_DAUGHTERS)
         return set_error(HPS_ERR_BAD_ARG, "n_daughters %d outside 2..10", ch->n_daughters);
+    if (ch->engine == HPS_ENGINE_MINSTD)
+        return set_error(HPS_ERR_BAD_ARG, "HPS_ENGINE_MINSTD channels are for hps_generate_range only");
     if (ch->engine != HPS_ENGINE_PHILOX && ch->engine != HPS_ENGINE_SQUARES3)
         return set_error(HPS_ERR_BAD_ARG, "unknown engine %d", ch->engine);
     std::memset(out, 0, sizeof(*out));
@@ -73,19 +75,6 @@ hps_status to_device_functor(const hps_functor* f, int n_daughters, DevFunctor* 
     return HPS_OK;
 }
 
-struct ConstCols { const double* p[HPS_MAX_DAUGHTERS]; };
-
-template <int N>
-__device__ __forceinline__ void load_event(const ConstCols& cols, uint64_t e, double (&p)[N][4])
-{
-#pragma unroll
-    for (int k = 0; k < N; ++k) {
-        const double2 a = __ldg(reinterpret_cast<const double2*>(cols.p[k] + 4 * e));
-        const double2 b = __ldg(reinterpret_cast<const double2*>(cols.p[k] + 4 * e) + 1);
-        p[k][0] = a.x; p[k][1] = a.y; p[k][2] = b.x; p[k][3] = b.y;
-    }
-}
-
 template <int N>
 __global__ void __launch_bounds__(256)
 k_event_weights(ConstCols cols, DevChannel ch, uint64_t n, double* __restrict__ out)
@@ -127,7 +116,7 @@ k_rng_words(uint64_t key, uint64_t first, uint64_t n, uint64_t* __restrict__ out
     }
 }
 
-static hps_status stored_event_args(int32_t n_daughters, const double* masses, uint64_t n,
+hps_status stored_event_args(int32_t n_daughters, const double* masses, uint64_t n,
                                     const double* const* cols, ConstCols* cc, DevChannel* ch,
                                     double max_weight)
 {

@@ -11,12 +11,47 @@
 //     per counter, counters evt+3N, evt+3N+1, ...
 //   * uniform on [0,1)            hydra_thrust/random/detail/uniform_real_distribution.inl:70-79:
 //     double(x) / 2^64 (Philox: double(2^64-1) rounds to 2^64) or x / 2^32 (squares3).
+//   * thrust's default_random_engine (minstd_rand), used only by phase_space_range
+//     (hydra/detail/PhaseSpaceRange.inl:46-73): x <- 48271 x mod 2^31-1, seeded with seed mod
+//     2^31-1 (0 -> 1), discard(z) = multiply by 48271^z; uniform = double(x - 1) / 2147483646.
 #pragma once
 #include <cstdint>
 
 namespace hps {
 
-enum : int { kPhilox = 0, kSquares3 = 1 };
+enum : int { kPhilox = 0, kSquares3 = 1, kMinstd = 2 };
+
+// minstd_rand arithmetic modulo the Mersenne prime 2^31 - 1: x < 2^62 folds as
+// (x mod 2^31) + (x >> 31), twice, then one conditional subtraction; exact.
+constexpr uint32_t kLcgA = 48271u;
+constexpr uint32_t kLcgM = 2147483647u;
+
+__host__ __device__ __forceinline__ uint32_t lcg_mulmod(uint32_t a, uint32_t b)
+{
+    uint64_t x = static_cast<uint64_t>(a) * b;
+    x = (x & kLcgM) + (x >> 31);
+    x = (x & kLcgM) + (x >> 31);
+    return static_cast<uint32_t>(x >= kLcgM ? x - kLcgM : x);
+}
+
+// 48271^z mod 2^31 - 1 by square-and-multiply.
+__host__ __device__ __forceinline__ uint32_t lcg_pow(uint64_t z)
+{
+    uint32_t acc = 1u, mult = kLcgA;
+    while (z) {
+        if (z & 1u) acc = lcg_mulmod(acc, mult);
+        mult = lcg_mulmod(mult, mult);
+        z >>= 1;
+    }
+    return acc;
+}
+
+// The engine state after seeding: the 32-bit seed reduced mod 2^31 - 1, 0 mapped to 1.
+__host__ __device__ __forceinline__ uint32_t lcg_seed_state(uint64_t seed)
+{
+    const uint32_t s = static_cast<uint32_t>(seed) % kLcgM;
+    return s == 0u ? 1u : s;
+}
 
 __host__ __device__ __forceinline__ uint64_t splitmix64(uint64_t x)
 {
@@ -74,6 +109,15 @@ __device__ __forceinline__ void stream_words(uint64_t key, uint64_t base, uint64
             w[2 * b] = o0;
             if (2 * b + 1 < NW) w[2 * b + 1] = o1;
         }
+    } else if constexpr (ENGINE == kMinstd) {
+        // key = seeded state; the first draw after discard(base) is state * 48271^(base+1)
+        uint32_t x = lcg_mulmod(static_cast<uint32_t>(key), lcg_pow(base + 1u));
+        w[0] = x;
+#pragma unroll
+        for (int k = 1; k < NW; ++k) {
+            x = lcg_mulmod(x, kLcgA);
+            w[k] = x;
+        }
     } else {
 #pragma unroll
         for (int k = 0; k < NW; ++k) w[k] = squares3_word(key, base + k);
@@ -91,6 +135,8 @@ template <int ENGINE>
 __device__ __forceinline__ double word_to_uniform(uint64_t x)
 {
     if constexpr (ENGINE == kPhilox) return __ull2double_rn(x) * 0x1p-64;
+    else if constexpr (ENGINE == kMinstd)
+        return __ddiv_rn(static_cast<double>(static_cast<uint32_t>(x) - 1u), 2147483646.0);
     else return static_cast<double>(static_cast<uint32_t>(x)) * 0x1p-32;
 }
 

@@ -56,8 +56,11 @@ typedef enum hps_status {
 typedef enum hps_engine {
     HPS_ENGINE_PHILOX = 0,    /* hydra::philox  = EngineR123<Philox2x64>, 7 rounds
                                  (hydra/detail/random/EngineR123.h:244, hydra_R123/philox.h:266) */
-    HPS_ENGINE_SQUARES3 = 1   /* hydra::default_random_engine = squares3
+    HPS_ENGINE_SQUARES3 = 1,  /* hydra::default_random_engine = squares3
                                  (hydra/detail/PRNGTypedefs.h:59, random/squares3.h:67) */
+    HPS_ENGINE_MINSTD = 2     /* thrust::random::default_random_engine = minstd_rand
+                                 (hydra_thrust/random/linear_congruential_engine.h:279), the engine
+                                 of phase_space_range only: accepted by hps_generate_range alone */
 } hps_engine;
 
 /* Arithmetic of the kinematics.  FP64 follows the reference in IEEE double;
@@ -232,6 +235,71 @@ hps_status hps_unweight_compact(int32_t n_daughters, uint64_t n, const double* c
                                 const double* weights_in, const uint8_t* flags, double* const* cols_out,
                                 double* weights_out, uint64_t* n_accepted, void* workspace,
                                 size_t workspace_bytes, void* stream);
+
+/* PhaseSpaceReweight (hydra/detail/Decays.inl:258-411) over a stored sample: out[e] =
+ * PhaseSpaceWeight(event e) * functor(event e), the value Decays::Unweight(functor, ...) tests
+ * (Decays.inl:472-476).  out may be NULL.  max_out (device, may be NULL) receives the largest
+ * value, as thrust::max_element over the same values gives it (Decays.inl:472-474); it is also
+ * used as 8 bytes of scratch while the call runs. */
+hps_status hps_reweight(int32_t n_daughters, const double* masses, double max_weight, const hps_functor* functor,
+                        uint64_t n, const double* const* cols, double* out, double* max_out, void* stream);
+
+/* Hit-or-miss flags from a weight column: flags[e] = weights[e] / W > u(first_evt + e), u the
+ * squares3(unweight_seed) uniform after discard(first_evt + e) (FlagDaugthers,
+ * Decays.inl:75-89).  W = *max_weight_dev when that device pointer is given (the max_out of
+ * hps_reweight), else max_weight.  With hps_reweight and hps_unweight_compact this is
+ * Decays::Unweight(functor, weight, seed) (Decays.inl:458-511). */
+hps_status hps_weight_flags(uint64_t n, const double* weights, double max_weight, const double* max_weight_dev,
+                            uint64_t unweight_seed, uint64_t first_evt, uint8_t* flags, void* stream);
+
+/* Two-dimensional dense histogram of two invariant masses squared, as
+ * DenseHistogram<double,2>::Fill(data, weights) (hydra/detail/DenseHistogram.inl:45-103) fills it
+ * with data = (m2(p[pair_a0] + p[pair_a1]), m2(p[pair_b0] + p[pair_b1])) -- the Dalitz plot of the
+ * reference's phsp_basic example.  Binning is GetGlobalBin's (functors/GetGlobalBin.h:120-138):
+ * x_d -> (x_d - lower_d) * grid_d / (upper_d - lower_d); both below 0 -> bin grid0*grid1
+ * (underflow), both above grid_d -> grid0*grid1 + 1 (overflow), else x0_bin * grid1 + x1_bin.  A
+ * point with one coordinate outside [0, grid_d) and the other not, which the reference maps through
+ * an undefined conversion, goes to the overflow bin.  bins has grid0*grid1 + 2 doubles and is
+ * overwritten, as Fill overwrites.  Bin sums are formed with atomic additions, so they agree with
+ * the reference's in-order sums to rounding (about 1e-15 relative), not bit for bit. */
+typedef struct hps_hist2d {
+    int32_t pair_a[2];
+    int32_t pair_b[2];
+    uint64_t grid[2];
+    double lower[2];
+    double upper[2];
+} hps_hist2d;
+
+typedef enum hps_hist_weight {
+    HPS_HIST_UNIT = 0,          /* weight 1 */
+    HPS_HIST_COLUMN = 1,        /* weights[e] */
+    HPS_HIST_PHSP_WEIGHT = 2    /* PhaseSpaceWeight recomputed from the event (Decays.inl:215-231),
+                                   the example's dalitz_weights; hps_generate_dalitz: the
+                                   generation-time weight instead */
+} hps_hist_weight;
+
+hps_status hps_dalitz_histogram(int32_t n_daughters, const double* masses, double max_weight, uint64_t n,
+                                const double* const* cols, const double* weights, int32_t weight_mode,
+                                const hps_hist2d* hist, double* bins, void* stream);
+
+/* Generate + histogram fused (FP64): the events of hps_generate(channel, first_evt, n) binned as
+ * hps_dalitz_histogram bins them, never stored.  weight_mode HPS_HIST_UNIT or
+ * HPS_HIST_PHSP_WEIGHT (the generation-time weight, which differs from the recomputed
+ * PhaseSpaceWeight by rounding only). */
+hps_status hps_generate_dalitz(const hps_channel* channel, uint64_t first_evt, uint64_t n, int32_t weight_mode,
+                               const hps_hist2d* hist, double* bins, void* stream);
+
+/* phase_space_range (hydra/detail/PhaseSpaceRange.inl:46-73): the lazy range of GenerateDecay
+ * (functors/GenerateDecay.h:222-334) with thrust's minstd_rand.  hps_range_channel sets up the
+ * channel as GenerateDecay's constructor does: ECM = mother.mass() - sum(m_i), the maximum weight
+ * from mother.mass(), the final-boost vector of the moving-mother quirk, seed truncated to the
+ * 32-bit GInt_t and engine HPS_ENGINE_MINSTD.  Where GenerateDecay has no checks this returns
+ * HPS_ERR_BAD_ARG (a mass <= 0) or HPS_ERR_NO_ENERGY.  hps_generate_range materialises events
+ * [first_evt, first_evt + n) of the range: element e is (weights[e], cols[0][e], ...). */
+hps_status hps_range_channel(hps_channel* ch, int32_t n_daughters, const double* masses, const double* mother,
+                             uint64_t seed);
+hps_status hps_generate_range(const hps_channel* ch, uint64_t first_evt, uint64_t n, double* const* cols,
+                              double* weights, void* stream);
 
 /* Raw random words of each event's stream (parity instrument): out[e*(3N-4)+k] is the k-th
  * word the reference engine returns for event first_evt+e (EngineR123.h:149-166 returns 64-bit

@@ -107,14 +107,41 @@ typedef struct {
     uint64_t cache[2];
     int trigger;
     uint64_t sq_state;   /* squares3 counter */
+    uint32_t lcg;        /* minstd_rand state */
 } hpso_stream;
+
+/* thrust's default_random_engine, minstd_rand: x <- 48271 x mod (2^31 - 1)
+ * (hydra_thrust/random/linear_congruential_engine.h:279).  Seeding reduces the 32-bit seed mod
+ * 2^31 - 1 and maps 0 to 1 (linear_congruential_engine.inl:41-50); discard(z) multiplies the state by
+ * 48271^z mod 2^31 - 1 (linear_congruential_engine_discard.h:47-74).  All products below fit 64 bits. */
+#define HPSO_LCG_A 48271u
+#define HPSO_LCG_M 2147483647u
+
+static inline uint32_t lcg_seed(uint64_t seed)
+{
+    uint32_t s = (uint32_t)seed % HPSO_LCG_M;
+    return s == 0 ? 1u : s;
+}
+
+static inline uint32_t lcg_discard(uint32_t state, uint64_t z)
+{
+    uint64_t mult = HPSO_LCG_A, acc = 1;
+    while (z > 0) {
+        if (z & 1) acc = (acc * mult) % HPSO_LCG_M;
+        z >>= 1;
+        mult = (mult * mult) % HPSO_LCG_M;
+    }
+    return (uint32_t)((acc * state) % HPSO_LCG_M);
+}
 
 static inline void stream_init(hpso_stream* s, int engine, uint64_t seed, uint64_t skip)
 {
     memset(s, 0, sizeof(*s));
     s->engine = engine;
     s->key = splitmix64(seed);
-    if (engine == 0) {
+    if (engine == 2) {
+        s->lcg = lcg_discard(lcg_seed(seed), skip);
+    } else if (engine == 0) {
         s->c0 = skip;                  /* incr(n) from {0,0}: carry only on wrap */
         s->c1 = 0;
         s->trigger = 2;
@@ -134,6 +161,10 @@ static inline uint64_t stream_word(hpso_stream* s)
         }
         return s->cache[s->trigger++];
     }
+    if (s->engine == 2) {
+        s->lcg = (uint32_t)(((uint64_t)s->lcg * HPSO_LCG_A) % HPSO_LCG_M);
+        return s->lcg;
+    }
     uint32_t w = squares3_word(s->key, s->sq_state);
     s->sq_state += 1;
     return (uint64_t)w;
@@ -142,9 +173,15 @@ static inline uint64_t stream_word(hpso_stream* s)
 static inline double stream_uniform(hpso_stream* s)
 {
     uint64_t w = stream_word(s);
-    double r = (double)w;
-    if (s->engine == 0) r /= 18446744073709551616.0;   /* 1 + double(2^64 - 1) == 2^64 */
-    else r /= 4294967296.0;                             /* 1 + double(2^32 - 1) == 2^32 */
+    double r;
+    if (s->engine == 2) {
+        r = (double)(uint32_t)(w - 1u);                 /* urng() - min, min = 1 */
+        r /= 2147483646.0;                              /* 1 + double(max - min) */
+    } else {
+        r = (double)w;
+        if (s->engine == 0) r /= 18446744073709551616.0;   /* 1 + double(2^64 - 1) == 2^64 */
+        else r /= 4294967296.0;                             /* 1 + double(2^32 - 1) == 2^32 */
+    }
     return r * (1.0 - 0.0) + 0.0;
 }
 
@@ -407,6 +444,77 @@ void hpso_recompute_weights(int n_daughters, const double* masses, double max_we
         out[e] = w;
     }
     (void)nthreads;
+}
+
+/* PhaseSpaceReweight::Evaluate (hydra/detail/Decays.inl:372-386): the PhaseSpaceWeight of each
+ * stored event times the functor of its daughters, w * f(p). */
+void hpso_reweight(int n_daughters, const double* masses, double max_weight, const hpso_functor* f,
+                   uint64_t n, const double* four, double* out, int nthreads)
+{
+    const int N = n_daughters;
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+#endif
+    for (int64_t e = 0; e < (int64_t)n; ++e) {
+        double p[HPSO_MAXN][4], R[4], S[4];
+        for (int i = 0; i < N; ++i) memcpy(p[i], four + (((size_t)i * n + (size_t)e) * 4), sizeof(p[i]));
+        memcpy(R, p[0], sizeof(R));
+        double w = max_weight;
+        for (int i = 1; i < N; ++i) {
+            for (int c = 0; c < 4; ++c) S[c] = R[c] + p[i][c];
+            w *= pdk(mass_of(S), masses[i], mass_of(R));
+            for (int c = 0; c < 4; ++c) R[c] += p[i][c];
+        }
+        out[e] = w * functor_eval(f, p);
+    }
+    (void)nthreads;
+}
+
+/* GetGlobalBin (hydra/detail/functors/GetGlobalBin.h:120-138) for two dimensions: x_d is mapped to
+ * (x_d - lo_d) * grid_d / (hi_d - lo_d); all coordinates below 0 -> bin g0*g1 (underflow), all above
+ * grid_d -> g0*g1 + 1 (overflow), otherwise size_t(x0) * g1 + size_t(x1).  The reference converts a
+ * negative coordinate to size_t there (undefined) and lets an index of g_d land in another row; this
+ * restatement sends every point with any coordinate outside [0, g_d) (and not all below / all above)
+ * to the overflow bin, as the CUDA kernel does. */
+static inline uint64_t global_bin2(const double x[2], const uint64_t g[2], const double lo[2], const double hi[2])
+{
+    double X[2];
+    int under = 1, over = 1, inside = 1;
+    for (int d = 0; d < 2; ++d) {
+        X[d] = (x[d] - lo[d]) * (double)g[d] / (hi[d] - lo[d]);
+        under = under && (X[d] < 0.0);
+        over = over && (X[d] > (double)g[d]);
+        inside = inside && (X[d] >= 0.0) && (X[d] < (double)g[d]);
+    }
+    const uint64_t nb = g[0] * g[1];
+    if (under) return nb;
+    if (over || !inside) return nb + 1;
+    return (uint64_t)X[0] * g[1] + (uint64_t)X[1];
+}
+
+/* DenseHistogram<double,2>::Fill(data, weights) (hydra/detail/DenseHistogram.inl:45-103) of the
+ * Dalitz variables (m2(p_a0 + p_a1), m2(p_b0 + p_b1)) of stored events, weighted by w[e] (NULL: 1).
+ * bins has g0*g1 + 2 entries and is overwritten; sums run in event order per bin, as the
+ * reference's sort_by_key + reduce_by_key does on a sequential backend. */
+void hpso_dalitz_histogram(int n_daughters, uint64_t n, const double* four, const double* w,
+                           const int32_t pairs[4], const uint64_t grid[2], const double lo[2],
+                           const double hi[2], double* bins)
+{
+    const uint64_t nb = grid[0] * grid[1] + 2;
+    for (uint64_t b = 0; b < nb; ++b) bins[b] = 0.0;
+    for (uint64_t e = 0; e < n; ++e) {
+        double x[2];
+        for (int d = 0; d < 2; ++d) {
+            const double* a = four + (((size_t)pairs[2 * d] * n + e) * 4);
+            const double* b = four + (((size_t)pairs[2 * d + 1] * n + e) * 4);
+            double s[4];
+            for (int c = 0; c < 4; ++c) s[c] = a[c] + b[c];
+            x[d] = mass2_of(s);
+        }
+        bins[global_bin2(x, grid, lo, hi)] += w ? w[e] : 1.0;
+    }
+    (void)n_daughters;
 }
 
 /* Hit-or-miss flags as Decays::Unweight: squares3(useed), discard(index),

@@ -26,6 +26,8 @@ SRC = HERE / "genbod_oracle.c"
 MAXN = 10
 ENGINE_PHILOX = 0
 ENGINE_SQUARES3 = 1
+ENGINE_MINSTD = 2          # thrust default_random_engine, phase_space_range only
+DEFAULT_FUNCTOR_UNWEIGHT_SEED = 0x39ABDC4529B1661C   # hydra/Decays.h:261
 DEFAULT_UNWEIGHT_SEED = 0x180EC6D33CFD0ABA   # hydra/Decays.h:253
 
 
@@ -89,8 +91,10 @@ def lib():
         L.hpso_generate_mothers.argtypes = [P(Channel), u64, u64, vp, vp, vp, i32]
         L.hpso_average_mothers.argtypes = [P(Channel), P(Functor), u64, u64, vp, vp]
         L.hpso_evaluate_mothers.argtypes = [P(Channel), P(Functor), u64, u64, vp, vp, vp, vp, i32]
+        L.hpso_reweight.argtypes = [i32, vp, dbl, P(Functor), u64, vp, vp, i32]
+        L.hpso_dalitz_histogram.argtypes = [i32, u64, vp, vp, vp, vp, vp, vp, vp]
         L.hpso_max_threads.restype = i32
-        for f in ("hpso_rng_words", "hpso_generate", "hpso_recompute_weights", "hpso_flags",
+        for f in ("hpso_reweight", "hpso_dalitz_histogram", "hpso_rng_words", "hpso_generate", "hpso_recompute_weights", "hpso_flags",
                   "hpso_evaluate", "hpso_average_on", "hpso_store_step", "hpso_unweight_uniforms",
                   "hpso_generate_mothers", "hpso_average_mothers", "hpso_evaluate_mothers"):
             getattr(L, f).restype = None
@@ -219,6 +223,55 @@ def evaluate_mothers(ch: Channel, fn: Functor, first: int, mothers: np.ndarray, 
     lib().hpso_evaluate_mothers(ctypes.byref(ch), ctypes.byref(fn), first, n, _ptr(mothers), _ptr(w), _ptr(f),
                                 _ptr(four), nthreads)
     return w, f, four
+
+
+def reweight(ch: Channel, fn: Functor, four: np.ndarray, max_weight=None, nthreads: int = 0) -> np.ndarray:
+    """PhaseSpaceReweight of stored events [N, n, 4]: PhaseSpaceWeight * functor."""
+    four = np.ascontiguousarray(four, dtype=np.float64)
+    n = four.shape[1]
+    out = np.zeros(n, dtype=np.float64)
+    m = np.ascontiguousarray(ch.masses, dtype=np.float64)
+    mw = ch.max_weight if max_weight is None else max_weight
+    lib().hpso_reweight(ch.n_daughters, _ptr(m), mw, ctypes.byref(fn), n, _ptr(four), _ptr(out), nthreads)
+    return out
+
+
+def unweight_functor(ch: Channel, fn: Functor, four: np.ndarray, weight: float = -1.0,
+                     seed: int = DEFAULT_FUNCTOR_UNWEIGHT_SEED, first: int = 0):
+    """Decays::Unweight(functor, weight, seed): (reweights, max value used, flags, permutation)."""
+    rw = reweight(ch, fn, four)
+    mv = float(weight) if weight > 0.0 else float(rw.max())
+    fl = flags(rw, mv, seed, first)
+    perm = np.concatenate([np.flatnonzero(fl), np.flatnonzero(fl == 0)])
+    return rw, mv, fl, perm
+
+
+def dalitz_histogram(four: np.ndarray, weights, pairs, grid, lower, upper) -> np.ndarray:
+    """2-D DenseHistogram::Fill of (m2(p_a0+p_a1), m2(p_b0+p_b1)); weights None -> 1."""
+    four = np.ascontiguousarray(four, dtype=np.float64)
+    n = four.shape[1]
+    pr = np.ascontiguousarray(pairs, dtype=np.int32)
+    g = np.ascontiguousarray(grid, dtype=np.uint64)
+    lo = np.ascontiguousarray(lower, dtype=np.float64)
+    hi = np.ascontiguousarray(upper, dtype=np.float64)
+    bins = np.zeros(int(g[0] * g[1]) + 2, dtype=np.float64)
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+    lib().hpso_dalitz_histogram(four.shape[0], n, _ptr(four), None if w is None else _ptr(w), _ptr(pr),
+                                _ptr(g), _ptr(lo), _ptr(hi), _ptr(bins))
+    return bins
+
+
+def mother_mass(mother) -> float:
+    """Vector4R::mass(): sqrt(E^2 - px^2 - py^2 - pz^2) when positive, else 0."""
+    E, px, py, pz = (float(x) for x in mother)
+    m2 = E * E - px * px - py * py - pz * pz
+    return float(np.sqrt(m2)) if m2 > 0.0 else 0.0
+
+
+def range_channel(masses, mother, seed) -> Channel:
+    """GenerateDecay's constructor (functors/GenerateDecay.h:121-160): ECM and maximum weight
+    from mother.mass(), the moving-mother boost vector, the seed cut to 32 bits, minstd_rand."""
+    return make_channel(masses, mother_mass(mother), int(seed) & 0xFFFFFFFF, ENGINE_MINSTD, mother)
 
 
 def max_threads() -> int:

@@ -16,6 +16,10 @@
  *   hydra/detail/Decays.inl:75-89          FlagDaugthers (hit-or-miss flag)
  *   hydra/detail/Decays.inl:415-455        Decays::Unweight()
  *   hydra/detail/random/EngineR123.h:97-172, squares3.h:105-125  raw RNG words
+ *   hydra/detail/Decays.inl:258-411, 458-511  PhaseSpaceReweight, Decays::Unweight(functor, w, seed)
+ *   hydra/detail/DenseHistogram.inl:45-103  2-D DenseHistogram::Fill(data, weights)
+ *   hydra/detail/PhaseSpaceRange.inl:46-73  phase_space_range (GenerateDecay, thrust minstd_rand)
+ *   hydra/detail/PhaseSpaceIntegrator.inl:37-42  PhaseSpaceIntegrator::Integrate
  *
  * Usage:
  *   ref_harness rng  N engine seed n                      out.bin
@@ -23,6 +27,8 @@
  *   ref_harness avg  N engine seed n M m0..m{N-1} fsel fi fj fa fb out.bin
  *   ref_harness time N engine seed n M m0..m{N-1} fsel fi fj fa fb reps
  *   ref_harness mothers N engine seed n M m0..m{N-1} fsel fi fj fa fb out.bin
+ *   ref_harness extras N engine seed n M m0..m{N-1} fsel fi fj fa fb fseed fmax g0 g1 lo0 lo1 hi0 hi1
+ *                      rseed mx my mz out.bin
  * engine: 0 = hydra::philox (Philox2x64, 7 rounds), 1 = hydra::default_random_engine (squares3)
  * fsel:   0 = constant 1, 1 = mass2(p_i+p_j), 2 = 1/((a^2 - mass2(p_i+p_j))^2 + (a*b)^2)
  * seed:   gen/avg/time: passed to PhaseSpace::SetSeed(GInt_t), -1 keeps the default (hash) seed;
@@ -36,6 +42,8 @@
 #include <hydra/Tuple.h>
 #include <hydra/multivector.h>
 #include <hydra/Range.h>
+#include <hydra/DenseHistogram.h>
+#include <hydra/PhaseSpaceIntegrator.h>
 #include <hydra/Placeholders.h>
 #include <hydra/host/System.h>
 #include <hydra/device/System.h>
@@ -48,6 +56,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <utility>
 #include <vector>
 
 declarg(D0, hydra::Vector4R)
@@ -116,6 +125,16 @@ inline double fmenu(FSpec const& f, hydra::Vector4R const* p)
 #define LAM_NAMES_10 LAM_NAMES_9, p9
 #define LAM_NAMES_11 LAM_NAMES_10, p10
 
+#define TLAM_ARGS_2  D0 p0, D1 p1
+#define TLAM_ARGS_3  TLAM_ARGS_2, D2 p2
+#define TLAM_ARGS_4  TLAM_ARGS_3, D3 p3
+#define TLAM_ARGS_5  TLAM_ARGS_4, D4 p4
+#define TLAM_ARGS_6  TLAM_ARGS_5, D5 p5
+#define TLAM_ARGS_7  TLAM_ARGS_6, D6 p6
+#define TLAM_ARGS_8  TLAM_ARGS_7, D7 p7
+#define TLAM_ARGS_9  TLAM_ARGS_8, D8 p8
+#define TLAM_ARGS_10 TLAM_ARGS_9, D9 p9
+
 template <size_t N> struct menu_lambda;
 #define MENU_LAMBDA(NN)                                                        \
     template <> struct menu_lambda<NN> {                                       \
@@ -128,6 +147,36 @@ template <size_t N> struct menu_lambda;
     };
 MENU_LAMBDA(2) MENU_LAMBDA(3) MENU_LAMBDA(4) MENU_LAMBDA(5) MENU_LAMBDA(6)
 MENU_LAMBDA(7) MENU_LAMBDA(8) MENU_LAMBDA(9) MENU_LAMBDA(10) MENU_LAMBDA(11)
+
+// The menu over the typed daughter columns: PhaseSpaceReweight hands its functor a tuple of the
+// Decays' own argument types (Decays.inl:383), which a lambda picks by type.
+template <size_t N> struct typed_menu_lambda;
+#define TYPED_MENU_LAMBDA(NN)                                                  \
+    template <> struct typed_menu_lambda<NN> {                                 \
+        static auto make(FSpec f) {                                            \
+            return hydra::wrap_lambda([f](TLAM_ARGS_##NN) {                    \
+                HV arr[NN] = {LAM_NAMES_##NN};                                 \
+                return fmenu(f, arr);                                          \
+            });                                                                \
+        }                                                                      \
+    };
+TYPED_MENU_LAMBDA(2) TYPED_MENU_LAMBDA(3) TYPED_MENU_LAMBDA(4) TYPED_MENU_LAMBDA(5) TYPED_MENU_LAMBDA(6)
+TYPED_MENU_LAMBDA(7) TYPED_MENU_LAMBDA(8) TYPED_MENU_LAMBDA(9) TYPED_MENU_LAMBDA(10)
+
+// (m^2(p0 + p1), m^2(p1 + p2)): the Dalitz variables of the reference's phsp_basic example.
+template <size_t N> struct dalitz_lambda;
+#define DALITZ_LAMBDA(NN)                                                      \
+    template <> struct dalitz_lambda<NN> {                                     \
+        static auto make() {                                                   \
+            return hydra::wrap_lambda([](TLAM_ARGS_##NN) {                     \
+                HV arr[NN] = {LAM_NAMES_##NN};                                 \
+                return hydra::make_tuple((arr[0] + arr[1]).mass2(),            \
+                                         (arr[1] + arr[2]).mass2());           \
+            });                                                                \
+        }                                                                      \
+    };
+DALITZ_LAMBDA(3) DALITZ_LAMBDA(4) DALITZ_LAMBDA(5) DALITZ_LAMBDA(6)
+DALITZ_LAMBDA(7) DALITZ_LAMBDA(8) DALITZ_LAMBDA(9) DALITZ_LAMBDA(10)
 
 template <typename T>
 void write_bin(const char* path, std::vector<T> const& v)
@@ -150,6 +199,11 @@ struct Args {
     FSpec f{0, 0, 1, 0.0, 0.0};
     unsigned long long useed = 0x180ec6d33cfd0abaULL;
     double mom[3] = {0, 0, 0};
+    unsigned long long fseed = 0x39abdc4529b1661cULL;
+    double fmax = -1.0;
+    size_t grid[2] = {0, 0};
+    double lo[2] = {0, 0}, hi[2] = {0, 0};
+    unsigned long long rseed = 0;
     const char* out = nullptr;
     int reps = 1;
 };
@@ -321,6 +375,95 @@ void run_mothers(Args const& a)
     write_bin(a.out, out);
 }
 
+template <size_t N>
+void push_events(std::vector<double>& out, hydra::Decays<typename ptypes<N>::type, hydra::host::sys_t>& ev, size_t n)
+{
+    for (size_t i = 0; i < n; ++i) {
+        auto t = ev[i];
+        hydra::Vector4R p[N];
+        hydra::detail::assignTupleToArray(t, p);
+        for (size_t k = 0; k < N; ++k)
+            for (int c = 0; c < 4; ++c) out.push_back(p[k].get(c));
+    }
+}
+
+template <typename Tup, size_t... K>
+void push_range_event(std::vector<double>& out, Tup const& t, std::index_sequence<K...>)
+{
+    out.push_back(hydra::get<0>(t));
+    hydra::Vector4R p[sizeof...(K)] = {hydra::get<K + 1>(t)...};
+    for (size_t k = 0; k < sizeof...(K); ++k)
+        for (int c = 0; c < 4; ++c) out.push_back(p[k].get(c));
+}
+
+// Consumers of a stored sample and the lazy generator.
+// layout: [n*N*4 Generate four-vectors (mother at rest)]
+//         [n PhaseSpaceReweight(functor) values]
+//         [n*N*4 after Unweight(functor, -1, fseed)] [kept]
+//         [n*N*4 after Unweight(functor, fmax, fseed)] [kept]
+//         [g0*g1+2 DenseHistogram<double,2> of (m2(p0+p1), m2(p1+p2)) weighted by PhaseSpaceWeight]
+//              (N >= 3 only)
+//         [n*(1+4N) phase_space_range(mother (E, mx, my, mz) of mass M, masses, rseed, n): weight, p...]
+//         [mean, err of PhaseSpaceIntegrator<N>(M, masses, n).Integrate(functor), its seed bits]
+template <size_t N, typename GRND>
+void run_extras(Args const& a)
+{
+    typedef typename ptypes<N>::type PT;
+    auto phsp = make_phsp<N, GRND>(a);
+    double masses[N];
+    std::array<double, N> amasses;
+    for (size_t i = 0; i < N; ++i) amasses[i] = masses[i] = a.m[i];
+    hydra::Vector4R rest(a.M, 0.0, 0.0, 0.0);
+    auto functor = menu_lambda<N>::make(a.f);
+    auto tfunctor = typed_menu_lambda<N>::make(a.f);
+    std::vector<double> out;
+
+    hydra::Decays<PT, hydra::host::sys_t> events(a.M, masses, a.n);
+    phsp.Generate(rest, events);
+    push_events<N>(out, events, a.n);
+    auto rw = events.GetEventWeightFunctor(tfunctor);
+    for (size_t i = 0; i < a.n; ++i) out.push_back(rw(events[i]));
+
+    for (int pass = 0; pass < 2; ++pass) {
+        hydra::Decays<PT, hydra::host::sys_t> ev2(a.M, masses, a.n);
+        phsp.Generate(rest, ev2);
+        auto kept = ev2.Unweight(tfunctor, pass == 0 ? -1.0 : a.fmax, static_cast<size_t>(a.fseed));
+        push_events<N>(out, ev2, a.n);
+        out.push_back(static_cast<double>(kept.size()));
+    }
+
+    if constexpr (N >= 3) {
+        auto dalitz_variables = events | dalitz_lambda<N>::make();
+        auto dalitz_weights = events | events.GetEventWeightFunctor();
+        auto hist = hydra::make_dense_histogram<double, 2>(hydra::host::sys, {a.grid[0], a.grid[1]},
+                                                            {a.lo[0], a.lo[1]}, {a.hi[0], a.hi[1]},
+                                                            dalitz_variables, dalitz_weights);
+        for (auto it = hist.begin(); it != hist.end(); ++it) out.push_back(*it);
+    }
+
+    {
+        const double E = std::sqrt(a.M * a.M + a.mom[0] * a.mom[0] + a.mom[1] * a.mom[1] + a.mom[2] * a.mom[2]);
+        hydra::Vector4R mother(E, a.mom[0], a.mom[1], a.mom[2]);
+        auto range = hydra::phase_space_range(mother, amasses, static_cast<size_t>(a.rseed), a.n);
+        auto first = range.begin();
+        for (size_t i = 0; i < a.n; ++i) push_range_event(out, first[i], std::make_index_sequence<N>{});
+    }
+
+    {
+        hydra::PhaseSpaceIntegrator<N, hydra::host::sys_t, GRND> integ(a.M, masses, a.n);
+        auto r = integ.Integrate(functor);
+        out.push_back(r.first);
+        out.push_back(r.second);
+        // the integrator's generator keeps the default seed; its bit pattern in a double slot
+        size_t dseed = 1;
+        dseed *= (1 + hydra::detail::hash_range(&masses[0], &masses[0] + N));
+        double dbits;
+        std::memcpy(&dbits, &dseed, sizeof(dbits));
+        out.push_back(dbits);
+    }
+    write_bin(a.out, out);
+}
+
 template <size_t N, typename GRND>
 void dispatch_mode(Args const& a)
 {
@@ -329,6 +472,7 @@ void dispatch_mode(Args const& a)
     else if (a.mode == "avg") run_avg<N, GRND>(a);
     else if (a.mode == "time") run_time<N, GRND>(a);
     else if (a.mode == "mothers") run_mothers<N, GRND>(a);
+    else if (a.mode == "extras") run_extras<N, GRND>(a);
     else { std::fprintf(stderr, "unknown mode %s\n", a.mode.c_str()); std::exit(2); }
 }
 
@@ -367,6 +511,16 @@ int main(int argc, char** argv)
         a.f.b = std::strtod(argv[k++], nullptr);
         if (a.mode == "gen") {
             a.useed = std::strtoull(argv[k++], nullptr, 0);
+            for (int c = 0; c < 3; ++c) a.mom[c] = std::strtod(argv[k++], nullptr);
+        }
+        if (a.mode == "extras") {
+            if (argc < k + 12) { std::fprintf(stderr, "missing args\n"); return 2; }
+            a.fseed = std::strtoull(argv[k++], nullptr, 0);
+            a.fmax = std::strtod(argv[k++], nullptr);
+            for (int c = 0; c < 2; ++c) a.grid[c] = std::strtoull(argv[k++], nullptr, 0);
+            for (int c = 0; c < 2; ++c) a.lo[c] = std::strtod(argv[k++], nullptr);
+            for (int c = 0; c < 2; ++c) a.hi[c] = std::strtod(argv[k++], nullptr);
+            a.rseed = std::strtoull(argv[k++], nullptr, 0);
             for (int c = 0; c < 3; ++c) a.mom[c] = std::strtod(argv[k++], nullptr);
         }
     }

@@ -55,6 +55,31 @@ AVG_CASES = [
 ]
 
 
+# Consumers of a stored sample and the lazy generator (ref_harness "extras"):
+# (name, N, engine, seed, n, M, masses, functor, fixed max weight for Unweight(functor, w), grid,
+#  phase_space_range seed, range mother momentum)
+FUNCTOR_UNWEIGHT_SEED = 0x39ABDC4529B1661C   # hydra/Decays.h:261 default
+EXTRA_CASES = [
+    ("extras_cfg1_n3_philox", 3, 0, 0x3039, 1024, 5.27934, [3.0969, K, PI], (2, 1, 2, 0.8955, 0.0473), 50.0,
+     (20, 25), 321, (0.1, -0.2, 0.3)),
+    ("extras_n5_squares3", 5, 1, 777, 512, 1.86484, [K, PI, PI, PI, PI], (1, 0, 1, 0.0, 0.0), 0.2,
+     (16, 12), 0xFFFFFFFF00000005, (0.0, 0.0, 0.0)),
+    ("extras_n2_philox", 2, 0, 5, 128, 3.0969, [0.10566, 0.10566], (0, 0, 1, 0.0, 0.0), 0.9,
+     (4, 4), 0, (0.5, 0.2, -1.0)),
+    ("extras_n10_philox", 10, 0, 0x3039, 128, 5.0, [PI] * 10, (2, 0, 1, 0.8955, 0.0473), 1e-6,
+     (10, 10), 2147483647, (0.0, 0.0, 0.0)),
+]
+
+
+def dalitz_limits(M, m):
+    """Kinematic limits of (m2(p0+p1), m2(p1+p2)), the example's histogram range."""
+    rest01 = sum(m[2:])
+    rest12 = m[0] + sum(m[3:])
+    lo = ((m[0] + m[1]) ** 2, (m[1] + m[2]) ** 2)
+    hi = ((M - rest01) ** 2, (M - rest12) ** 2)
+    return lo, hi
+
+
 # (name, N, engine, seed, n, M, masses, functor over (mother, daughters...))
 MOTHER_CASES = [
     ("mothers_n3_philox", 3, 0, 12345, 96, 5.27934, [3.0969, K, PI], (1, 0, 2, 0.0, 0.0)),
@@ -112,6 +137,40 @@ def main():
         o += n * N * 4
         fx["eval_w"], fx["eval_f"] = d[o:o + n], d[o + n:o + 2 * n]
         fx["avg_mean"], fx["avg_err"] = d[o + 2 * n], d[o + 2 * n + 1]
+        fixtures[name] = fx
+    for name, N, eng, seed, n, M, m, f, fmax, grid, rseed, mom in EXTRA_CASES:
+        if N >= 3:
+            lo, hi = dalitz_limits(M, m)
+        else:
+            lo, hi = (0.0, 0.0), (1.0, 1.0)
+        args = ["extras", N, eng, seed, n, fnum(M)] + [fnum(x) for x in m] + \
+               [f[0], f[1], f[2], fnum(f[3]), fnum(f[4]), hex(FUNCTOR_UNWEIGHT_SEED), fnum(fmax),
+                grid[0], grid[1], fnum(lo[0]), fnum(lo[1]), fnum(hi[0]), fnum(hi[1]), rseed] + [fnum(x) for x in mom]
+        d = np.fromfile(run(args, tmp), dtype=np.float64)
+        E = float(np.sqrt(M * M + sum(x * x for x in mom)))
+        fx = dict(N=N, engine=eng, seed=seed, n=n, M=M, masses=np.array(m), functor=np.array(f),
+                  fseed=np.uint64(FUNCTOR_UNWEIGHT_SEED), fmax=fmax, grid=np.array(grid, dtype=np.uint64),
+                  lower=np.array(lo), upper=np.array(hi), rseed=np.uint64(rseed), range_mother=np.array([E, *mom]))
+        nf = n * N * 4
+        o = 0
+
+        def four_at(o):
+            return d[o:o + nf].reshape(n, N, 4).transpose(1, 0, 2).copy()
+        fx["four"] = four_at(o); o += nf
+        fx["reweight"] = d[o:o + n]; o += n
+        fx["unw_max_four"] = four_at(o); o += nf
+        fx["unw_max_kept"] = int(d[o]); o += 1
+        fx["unw_fixed_four"] = four_at(o); o += nf
+        fx["unw_fixed_kept"] = int(d[o]); o += 1
+        if N >= 3:
+            nb = grid[0] * grid[1] + 2
+            fx["hist"] = d[o:o + nb]; o += nb
+        r = d[o:o + n * (1 + 4 * N)].reshape(n, 1 + 4 * N); o += n * (1 + 4 * N)
+        fx["range_w"] = r[:, 0].copy()
+        fx["range_four"] = r[:, 1:].reshape(n, N, 4).transpose(1, 0, 2).copy()
+        fx["integ_mean"], fx["integ_err"] = d[o], d[o + 1]
+        fx["integ_seed"] = d[o + 2:o + 3].view(np.uint64)[0]
+        assert o + 3 == len(d), (name, o, len(d))
         fixtures[name] = fx
     tmp.unlink()
     for name, fx in fixtures.items():

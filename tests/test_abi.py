@@ -113,3 +113,58 @@ def test_bad_arguments_rejected_before_launch(hps):
     assert st == hps.ERR_BAD_ARG and b"indices" in lib.hps_last_error()
     # n == 0 is a no-op, as an empty Thrust range
     assert lib.hps_generate(ctypes.byref(ch), 0, 0, None, None, None, 0, 0, None) == hps.OK
+
+
+@pytest.mark.parametrize("name", [n for n in __import__("conftest").EXTRA_GOLDEN])
+def test_range_channel_matches_generate_decay(hps, oracle, name):
+    """hps_range_channel sets up GenerateDecay's constructor exactly as the oracle does."""
+    from hydra_gb300 import api
+    g = load_golden(name)
+    ch = api.range_channel(list(g["masses"]), list(g["range_mother"]), int(g["rseed"]))
+    och = oracle.range_channel(g["masses"], g["range_mother"], int(g["rseed"]))
+    assert ch.engine == hps.ENGINE_MINSTD and ch.seed == och.seed == int(g["rseed"]) & 0xFFFFFFFF
+    assert ch.ecm == och.ecm and ch.max_weight == och.max_weight
+    assert list(ch.beta) == list(och.beta)
+
+
+def test_consumer_arguments_rejected_before_launch(hps):
+    from hydra_gb300 import api
+    lib = hps.lib()
+    cols = (ctypes.c_void_p * 3)(256, 512, 768)   # aligned, never dereferenced
+    m = (ctypes.c_double * 3)(0.1, 0.2, 0.3)
+    bins = ctypes.c_void_p(1024)
+    cases = [
+        (api.hist2d((0, 0), (1, 2), (10, 10), (0, 0), (1, 1)), b"same daughter"),
+        (api.hist2d((0, 1), (1, 3), (10, 10), (0, 0), (1, 1)), b"outside"),
+        (api.hist2d((0, 1), (1, 2), (0, 10), (0, 0), (1, 1)), b"grid"),
+        (api.hist2d((0, 1), (1, 2), (10, 10), (0, 1), (1, 1)), b"upper"),
+    ]
+    for h, msg in cases:
+        st = lib.hps_dalitz_histogram(3, ctypes.cast(m, ctypes.c_void_p), 1.0, 10, ctypes.cast(cols, ctypes.c_void_p),
+                                      None, 0, ctypes.byref(h), bins, None)
+        assert st == hps.ERR_BAD_ARG and msg in lib.hps_last_error(), msg
+    h = api.hist2d((0, 1), (1, 2), (10, 10), (0, 0), (1, 1))
+    st = lib.hps_dalitz_histogram(3, ctypes.cast(m, ctypes.c_void_p), 1.0, 10, ctypes.cast(cols, ctypes.c_void_p),
+                                  None, 9, ctypes.byref(h), bins, None)
+    assert st == hps.ERR_BAD_ARG and b"weight mode" in lib.hps_last_error()
+    st = lib.hps_dalitz_histogram(3, ctypes.cast(m, ctypes.c_void_p), 1.0, 10, ctypes.cast(cols, ctypes.c_void_p),
+                                  None, hps.HIST_COLUMN, ctypes.byref(h), bins, None)
+    assert st == hps.ERR_BAD_ARG and b"weights is NULL" in lib.hps_last_error()
+    # a minstd channel is for hps_generate_range only, and hps_generate_range takes nothing else
+    rch = api.range_channel([0.1, 0.2, 0.3], [2.0, 0.0, 0.0, 0.0], 5)
+    st = lib.hps_generate(ctypes.byref(rch), 0, 10, None, None, None, 0, 0, None)
+    assert st == hps.ERR_BAD_ARG and b"hps_generate_range" in lib.hps_last_error()
+    ch = api.make_channel([0.1, 0.2, 0.3], 1.0, 1)
+    st = lib.hps_generate_range(ctypes.byref(ch), 0, 10, ctypes.cast(cols, ctypes.c_void_p), None, None)
+    assert st == hps.ERR_BAD_ARG and b"hps_range_channel" in lib.hps_last_error()
+    st = lib.hps_generate_dalitz(ctypes.byref(ch), 0, 10, hps.HIST_COLUMN, ctypes.byref(h), bins, None)
+    assert st == hps.ERR_BAD_ARG
+    # GenerateDecay has no checks; the range set-up reports what would otherwise be NaNs
+    with pytest.raises(hps.HpsError):
+        api.range_channel([0.1, 0.2, 0.3], [0.5, 0.0, 0.0, 0.0], 5)
+    fn = hps.HpsFunctor(7, 0, 1, 0, 0.0, 0.0)
+    st = lib.hps_reweight(3, ctypes.cast(m, ctypes.c_void_p), 1.0, ctypes.byref(fn), 10,
+                          ctypes.cast(cols, ctypes.c_void_p), None, None, None)
+    assert st == hps.ERR_BAD_ARG and b"kind" in lib.hps_last_error()
+    st = lib.hps_weight_flags(10, None, 1.0, None, 0, 0, None, None)
+    assert st == hps.ERR_BAD_ARG

@@ -53,7 +53,9 @@ def test_mothers_match_reference(api, torch, oracle, name):
     assert np.allclose(ef.cpu().numpy(), g["eval_f"], rtol=TOL, atol=0)
     mean, m2, W = out.cpu().tolist()
     assert abs(mean - g["avg_mean"]) <= 1e-10 * abs(g["avg_mean"])
-    assert abs(np.sqrt(m2) / W - g["avg_err"]) <= 1e-8 * abs(g["avg_err"])
+    # the spread is rounding noise when the functor is constant (N=2: m2(p1+p2) is the mother
+    # mass squared), so the error also gets an absolute allowance at the scale of the mean
+    assert abs(np.sqrt(m2) / W - g["avg_err"]) <= 1e-8 * abs(g["avg_err"]) + 1e-12 * abs(mean)
 
 
 def test_decay_chain_from_daughter_column(api, torch, oracle):

@@ -13,7 +13,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from conftest import AVG_GOLDEN, GEN_GOLDEN, MOTHER_GOLDEN, REPO, RNG_GOLDEN, load_golden
+from conftest import AVG_GOLDEN, EXTRA_GOLDEN, GEN_GOLDEN, MOTHER_GOLDEN, REPO, RNG_GOLDEN, load_golden
 
 REF = REPO / "oracle" / "_ref" / "ref_harness_cpp"
 
@@ -150,3 +150,72 @@ def test_mothers_variants_bit_exact(oracle, name):
     assert np.array_equal(w, g["eval_w"]) and np.array_equal(fv, g["eval_f"])
     mean, m2, W = oracle.average_mothers(ch, fn, 0, g["mothers"])
     assert mean == g["avg_mean"] and np.sqrt(m2) / W == g["avg_err"]
+
+
+# ------------------------------------------------ consumers of a stored sample, lazy range --
+
+def _functor(O, g):
+    f = g["functor"]
+    return O.make_functor(int(f[0]), int(f[1]), int(f[2]), float(f[3]), float(f[4]))
+
+
+@pytest.mark.parametrize("name", EXTRA_GOLDEN)
+def test_reweight_and_unweight_functor_bit_exact(oracle, name):
+    """PhaseSpaceReweight values and both Unweight(functor, w, seed) permutations."""
+    g = load_golden(name)
+    ch = oracle.make_channel(g["masses"], float(g["M"]), int(g["seed"]), int(g["engine"]))
+    four, _ = oracle.generate(ch, 0, int(g["n"]))
+    assert np.array_equal(four, g["four"])
+    fn = _functor(oracle, g)
+    assert np.array_equal(oracle.reweight(ch, fn, four), g["reweight"])
+    for key, weight in (("unw_max", -1.0), ("unw_fixed", float(g["fmax"]))):
+        _, _, fl, perm = oracle.unweight_functor(ch, fn, four, weight, int(g["fseed"]))
+        assert int(fl.sum()) == int(g[key + "_kept"])
+        assert np.array_equal(four[:, perm], g[key + "_four"])
+
+
+@pytest.mark.parametrize("name", [n for n in EXTRA_GOLDEN if int(load_golden(n)["N"]) >= 3])
+def test_dalitz_histogram_bit_exact(oracle, name):
+    """DenseHistogram<double,2>::Fill of the Dalitz variables weighted by PhaseSpaceWeight."""
+    g = load_golden(name)
+    ch = oracle.make_channel(g["masses"], float(g["M"]), int(g["seed"]), int(g["engine"]))
+    w = oracle.recompute_weights(ch, g["four"])
+    bins = oracle.dalitz_histogram(g["four"], w, [0, 1, 1, 2], g["grid"], g["lower"], g["upper"])
+    assert np.array_equal(bins, g["hist"])
+    assert bins.sum() > 0
+
+
+@pytest.mark.parametrize("name", EXTRA_GOLDEN)
+def test_phase_space_range_bit_exact(oracle, name):
+    """phase_space_range: GenerateDecay over thrust's minstd_rand, 32-bit seed, mother-mass ECM."""
+    g = load_golden(name)
+    ch = oracle.range_channel(g["masses"], g["range_mother"], int(g["rseed"]))
+    four, w = oracle.generate(ch, 0, int(g["n"]))
+    assert np.array_equal(w, g["range_w"])
+    assert np.array_equal(four, g["range_four"])
+
+
+def test_minstd_words_against_recurrence(oracle):
+    """Event e of a minstd stream starts at seed * 48271^(e+3N+1) mod 2^31-1 (discard by modular
+    exponentiation); check it against the plain recurrence x <- 48271 x mod 2^31-1."""
+    m = 2**31 - 1
+    for seed in (987654321, 0, m, m + 5, 2**32 - 1):
+        N = 4
+        x = (seed & 0xFFFFFFFF) % m or 1
+        stream = []
+        for _ in range(40 + 6 * N):
+            x = x * 48271 % m
+            stream.append(x)
+        words = oracle.rng_words(N, oracle.ENGINE_MINSTD, seed, 0, 40)
+        for e in range(40):
+            assert list(words[e]) == stream[e + 3 * N:e + 3 * N + 3 * N - 4]
+
+
+@pytest.mark.parametrize("name", EXTRA_GOLDEN)
+def test_phase_space_integrator_sequential_fold(oracle, name):
+    """PhaseSpaceIntegrator::Integrate = AverageOn with the generator's default seed."""
+    g = load_golden(name)
+    ch = oracle.make_channel(g["masses"], float(g["M"]), int(g["integ_seed"]), int(g["engine"]))
+    mean, m2, w = oracle.average_on(ch, _functor(oracle, g), 0, int(g["n"]), nthreads=1)
+    assert mean == g["integ_mean"]
+    assert np.sqrt(m2) / w == g["integ_err"]
