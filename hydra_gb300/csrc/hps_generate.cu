@@ -236,6 +236,30 @@ extern "C" hps_status hps_generate_host(const hps_channel* channel, uint64_t fir
     if (!host_cols) return set_error(HPS_ERR_BAD_ARG, "host_cols is NULL");
     for (int k = 0; k < N; ++k)
         if (!host_cols[k]) return set_error(HPS_ERR_BAD_ARG, "host column %d is NULL", k);
+    if (chunk_events == 0) {
+        // Direct mode: when every host buffer is pinned, device-mapped memory, the kernel writes
+        // the Decays straight into it across the CPU-GPU link -- no staging copy, no copy engine.
+        double* dcols[HPS_MAX_DAUGHTERS];
+        bool mapped = true;
+        auto map = [&](void* h, void** d) {
+            if (!h) { *d = nullptr; return; }
+            if (cudaHostGetDevicePointer(d, h, 0) != cudaSuccess) {
+                cudaGetLastError();
+                mapped = false;
+            }
+        };
+        for (int k = 0; k < N && mapped; ++k) map(host_cols[k], reinterpret_cast<void**>(&dcols[k]));
+        void* dw = nullptr;
+        void* df = nullptr;
+        if (mapped) map(host_weights, &dw);
+        if (mapped) map(host_flags, &df);
+        if (mapped) {
+            st = hps_generate(channel, first_evt, n, dcols, static_cast<double*>(dw), static_cast<uint8_t*>(df),
+                              unweight_seed, precision, stream);
+            if (st != HPS_OK) return st;
+            return cuda_status(cudaStreamSynchronize(as_stream(stream)), "cudaStreamSynchronize");
+        }
+    }
     const uint64_t chunk = chunk_events ? chunk_events : (uint64_t(1) << 20);
     // staging: N columns of 32 B/event (32-byte aligned), then weights, then flags
     const size_t col_bytes = (size_t)chunk * 32;

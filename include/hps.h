@@ -143,11 +143,14 @@ hps_status hps_generate(const hps_channel* ch, uint64_t first_evt, uint64_t n,
 
 /* Generate into HOST memory: the GPU form of Generate(mother, Decays<..., hydra::host::sys_t>)
  * (PhaseSpace.inl:377-394 with a host-backend Decays).  Same outputs as hps_generate, but
- * host_cols / host_weights / host_flags are host pointers (pinned memory gives full link
- * bandwidth).  Events are produced in chunks of chunk_events (0 = library default) into two
- * device staging buffers taken from the stream-ordered allocator; each chunk's device->host
- * copies run on a second stream while the next chunk is generated.  Returns when all copies
- * are complete (synchronous, like the reference call). */
+ * host_cols / host_weights / host_flags are host pointers.
+ *   chunk_events == 0 and every buffer pinned, device-mapped memory (cudaHostAlloc, or
+ *     cudaHostRegister with the mapped flag): the kernel writes straight into host memory
+ *     across the CPU-GPU link, no staging.
+ *   otherwise: events are produced in chunks of chunk_events (0 = 2^20) into two device staging
+ *     buffers from the stream-ordered allocator; each chunk's device->host copies run on a second
+ *     stream while the next chunk is generated.
+ * Returns when the host memory holds the results (synchronous, like the reference call). */
 hps_status hps_generate_host(const hps_channel* ch, uint64_t first_evt, uint64_t n,
                              double* const* host_cols, double* host_weights, uint8_t* host_flags,
                              uint64_t unweight_seed, int32_t precision, uint64_t chunk_events,

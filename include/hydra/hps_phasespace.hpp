@@ -107,6 +107,10 @@ struct arg_base<T, false> {
 // ----------------------------------------------------------------------------- back-ends
 
 namespace detail {
+// tuple<double, Vector4R x N>: an element of phase_space_range
+template <size_t N, typename... T> struct tuple_cat_helper : tuple_cat_helper<N - 1, Vector4R, T...> {};
+template <typename... T> struct tuple_cat_helper<0, T...> { typedef std::tuple<double, T...> type; };
+
 struct HostBackend {};
 struct DeviceBackend {};
 
@@ -263,34 +267,110 @@ public:
     size_t Unweight(size_t seed = 0x180ec6d33cfd0abaULL)
     {
         if (!fN) return 0;
-        if (on_device) {
-            // flags and the stable partition stay on the device (hps_unweight_compact)
-            const double* cols[nparticles];
-            double* outc[nparticles];
-            detail::DeviceBuffer<double> out[nparticles];
-            for (size_t k = 0; k < nparticles; ++k) {
-                cols[k] = fDevCols[k].p;
-                out[k].resize(4 * fN);
-                outc[k] = out[k].p;
-            }
-            detail::DeviceBuffer<uint8_t> f(fN);
-            detail::DeviceBuffer<double> wout(fN);
-            detail::DeviceBuffer<uint64_t> nacc(1);
-            detail::throw_status(hps_unweight_flags(nparticles, fMasses, fMaxWeight, fN, cols, seed, 0, f.p, nullptr));
-            detail::throw_status(hps_unweight_compact(nparticles, fN, cols, fDevW.p, f.p, outc, wout.p, nacc.p,
-                                                      nullptr, 0, nullptr));
-            uint64_t kept = 0;
-            detail::throw_cuda(cudaMemcpy(&kept, nacc.p, sizeof(kept), cudaMemcpyDeviceToHost), "cudaMemcpy");
-            for (size_t k = 0; k < nparticles; ++k) std::swap(fDevCols[k], out[k]);
-            std::swap(fDevW, wout);
-            return static_cast<size_t>(kept);
-        }
         std::vector<uint8_t> flags(fN);
         with_device_columns([&](const double* const* cols) {
             detail::DeviceBuffer<uint8_t> f(fN);
             detail::throw_status(hps_unweight_flags(nparticles, fMasses, fMaxWeight, fN, cols, seed, 0, f.p, nullptr));
+            if (on_device) {
+                compact_device(f.p);       // flags and the stable partition stay on the device
+                return;
+            }
             detail::throw_cuda(cudaMemcpy(flags.data(), f.p, fN, cudaMemcpyDeviceToHost), "cudaMemcpy");
         });
+        if (on_device) return fKept;
+        return partition_host(flags);
+    }
+
+    // Events | Events.GetEventWeightFunctor(functor) (Decays.h:243-250): PhaseSpaceWeight times
+    // the functor, evaluated eagerly (PhaseSpaceReweight, Decays.inl:372-386).
+    template <typename Functor>
+    std::vector<double> GetEventWeights(Functor const& functor) const
+    {
+        static_assert(hps_fn::is_menu<Functor>::value, "the functor crosses the C ABI: hydra::hps_fn::One, Mass2, BW2");
+        std::vector<double> w(fN);
+        if (!fN) return w;
+        with_device_columns([&](const double* const* cols) {
+            detail::DeviceBuffer<double> out(fN);
+            detail::throw_status(hps_reweight(nparticles, fMasses, fMaxWeight, &functor.f, fN, cols, out.p, nullptr,
+                                              nullptr));
+            detail::throw_cuda(cudaMemcpy(w.data(), out.p, fN * 8, cudaMemcpyDeviceToHost), "cudaMemcpy");
+        });
+        return w;
+    }
+
+    // Decays::Unweight(functor, weight, seed) (Decays.inl:458-511): hit-or-miss on
+    // PhaseSpaceWeight * functor against weight, or against the largest such value when
+    // weight <= 0; accepted events move to the front in their original order; returns how many.
+    template <typename Functor>
+    size_t Unweight(Functor const& functor, double weight = -1.0, size_t seed = 0x39abdc4529b1661cULL)
+    {
+        static_assert(hps_fn::is_menu<Functor>::value, "the functor crosses the C ABI: hydra::hps_fn::One, Mass2, BW2");
+        if (!fN) return 0;
+        std::vector<uint8_t> flags(fN);
+        detail::DeviceBuffer<uint8_t> f(fN);
+        with_device_columns([&](const double* const* cols) {
+            detail::DeviceBuffer<double> rw(fN);
+            detail::DeviceBuffer<double> mx(1);
+            detail::throw_status(hps_reweight(nparticles, fMasses, fMaxWeight, &functor.f, fN, cols, rw.p, mx.p,
+                                              nullptr));
+            detail::throw_status(hps_weight_flags(fN, rw.p, weight, weight > 0.0 ? nullptr : mx.p, seed, 0, f.p,
+                                                  nullptr));
+            if (on_device) {
+                compact_device(f.p);
+                return;
+            }
+            detail::throw_cuda(cudaMemcpy(flags.data(), f.p, fN, cudaMemcpyDeviceToHost), "cudaMemcpy");
+        });
+        if (on_device) return fKept;
+        return partition_host(flags);
+    }
+
+    // Not in the reference as one call: the Dalitz plot of its phsp_basic example,
+    // make_dense_histogram<double,2>(sys, grid, lower, upper, Events | dalitz, Events | weights)
+    // with dalitz = (m2(p[a0] + p[a1]), m2(p[b0] + p[b1])) and the recomputed PhaseSpaceWeight.
+    // Returns grid[0]*grid[1] bin contents followed by the underflow and overflow bins.
+    std::vector<double> DalitzHistogram(std::array<size_t, 2> const& grid, std::array<double, 2> const& lower,
+                                        std::array<double, 2> const& upper, std::array<int, 2> const& pair_a = {0, 1},
+                                        std::array<int, 2> const& pair_b = {1, 2},
+                                        int32_t weight_mode = HPS_HIST_PHSP_WEIGHT) const
+    {
+        hps_hist2d h{{pair_a[0], pair_a[1]}, {pair_b[0], pair_b[1]}, {grid[0], grid[1]}, {lower[0], lower[1]},
+                     {upper[0], upper[1]}};
+        std::vector<double> bins(grid[0] * grid[1] + 2);
+        with_device_columns([&](const double* const* cols) {
+            detail::DeviceBuffer<double> b(bins.size());
+            detail::throw_status(hps_dalitz_histogram(nparticles, fMasses, fMaxWeight, fN, cols, nullptr, weight_mode,
+                                                      &h, b.p, nullptr));
+            detail::throw_cuda(cudaMemcpy(bins.data(), b.p, bins.size() * 8, cudaMemcpyDeviceToHost), "cudaMemcpy");
+        });
+        return bins;
+    }
+
+private:
+    // stable partition of the device columns by flags (hps_unweight_compact); sets fKept
+    void compact_device(const uint8_t* flags)
+    {
+        const double* cols[nparticles];
+        double* outc[nparticles];
+        detail::DeviceBuffer<double> out[nparticles];
+        for (size_t k = 0; k < nparticles; ++k) {
+            cols[k] = fDevCols[k].p;
+            out[k].resize(4 * fN);
+            outc[k] = out[k].p;
+        }
+        detail::DeviceBuffer<double> wout(fN);
+        detail::DeviceBuffer<uint64_t> nacc(1);
+        detail::throw_status(hps_unweight_compact(nparticles, fN, cols, fDevW.p, flags, outc, wout.p, nacc.p, nullptr,
+                                                  0, nullptr));
+        uint64_t kept = 0;
+        detail::throw_cuda(cudaMemcpy(&kept, nacc.p, sizeof(kept), cudaMemcpyDeviceToHost), "cudaMemcpy");
+        for (size_t k = 0; k < nparticles; ++k) std::swap(fDevCols[k], out[k]);
+        std::swap(fDevW, wout);
+        fKept = static_cast<size_t>(kept);
+    }
+
+    size_t partition_host(const std::vector<uint8_t>& flags)
+    {
         std::vector<size_t> order;
         order.reserve(fN);
         for (size_t i = 0; i < fN; ++i) if (flags[i]) order.push_back(i);
@@ -300,7 +380,6 @@ public:
         return kept;
     }
 
-private:
     template <size_t... I>
     static value_type make(const Vector4R (&p)[nparticles], std::index_sequence<I...>)
     {
@@ -367,6 +446,7 @@ private:
     double fMaxWeight = 0.0;
     double fMasses[HPS_MAX_DAUGHTERS] = {};
     size_t fN = 0;
+    size_t fKept = 0;
     detail::DeviceBuffer<double> fDevCols[nparticles];
     detail::DeviceBuffer<double> fDevW;
     std::vector<double> fHostCols[nparticles];
@@ -536,6 +616,119 @@ private:
     GReal_t fMasses[N] = {};
     int32_t fPrecision = HPS_PREC_FP64;
 };
+
+// -------------------------------------------------------------------- PhaseSpaceIntegrator
+
+// hydra::PhaseSpaceIntegrator<N, Backend, GRND> (hydra/PhaseSpaceIntegrator.h:52-160):
+// Integrate(functor) = AverageOn(mother at rest, functor, n) of a PhaseSpace that keeps the
+// default seed (PhaseSpaceIntegrator.inl:37-42).
+template <size_t N, typename Backend = device::sys_t, typename GRND = default_random_engine>
+class PhaseSpaceIntegrator {
+public:
+    PhaseSpaceIntegrator(double motherMass, const double (&daughtersMasses)[N], size_t n)
+        : fGenerator(motherMass, daughtersMasses), fMother(motherMass, 0, 0, 0), fNSamples(n) {}
+    PhaseSpaceIntegrator(double motherMass, std::array<GReal_t, N> const& daughtersMasses, size_t n)
+        : fGenerator(motherMass, daughtersMasses), fMother(motherMass, 0, 0, 0), fNSamples(n) {}
+    PhaseSpaceIntegrator(double motherMass, std::initializer_list<GReal_t> const& daughtersMasses, size_t n)
+        : fGenerator(motherMass, daughtersMasses), fMother(motherMass, 0, 0, 0), fNSamples(n) {}
+
+    template <typename Functor>
+    std::pair<GReal_t, GReal_t> Integrate(Functor const& functor)
+    {
+        return fGenerator.AverageOn(Backend{}, fMother, functor, fNSamples);
+    }
+
+    const PhaseSpace<N, GRND>& GetGenerator() const { return fGenerator; }
+    PhaseSpace<N, GRND>& GetGenerator() { return fGenerator; }
+    const Vector4R& GetMother() const { return fMother; }
+    void SetMother(Vector4R const& m) { fMother = m; }
+    size_t GetNSamples() const { return fNSamples; }
+    void SetNSamples(size_t n) { fNSamples = n; }
+
+private:
+    PhaseSpace<N, GRND> fGenerator;
+    Vector4R fMother;
+    size_t fNSamples;
+};
+
+// --------------------------------------------------------------------- phase_space_range
+
+// phase_space_range(mother, masses, seed, length) (hydra/detail/PhaseSpaceRange.inl:46-73): the
+// reference returns a lazy range of tuple(weight, Vector4R...) over GenerateDecay with thrust's
+// minstd_rand.  Here the range is materialised on the device when it is created (length must be
+// given: the reference's length 0 means "unbounded"), then read like the lazy one:
+// range[i] / begin()[i] is the same tuple.
+template <size_t N>
+class PhaseSpaceRange {
+public:
+    typedef typename detail::tuple_cat_helper<N>::type value_type;
+
+    PhaseSpaceRange(Vector4R const& mother, std::array<double, N> const& masses, size_t seed, size_t length)
+        : fN(length)
+    {
+        if (length == 0) throw std::invalid_argument("phase_space_range: a materialised range needs its length");
+        hps_channel ch;
+        detail::throw_status(hps_range_channel(&ch, N, masses.data(), mother.data(), seed));
+        double* cols[N];
+        for (size_t k = 0; k < N; ++k) {
+            fCols[k].resize(4 * length);
+            cols[k] = fCols[k].p;
+        }
+        fW.resize(length);
+        detail::throw_status(hps_generate_range(&ch, 0, length, cols, fW.p, nullptr));
+        detail::throw_cuda(cudaStreamSynchronize(nullptr), "cudaStreamSynchronize");
+    }
+
+    size_t size() const { return fN; }
+
+    value_type operator[](size_t i) const
+    {
+        double w;
+        Vector4R p[N];
+        detail::throw_cuda(cudaMemcpy(&w, fW.p + i, 8, cudaMemcpyDeviceToHost), "cudaMemcpy");
+        for (size_t k = 0; k < N; ++k) {
+            double v[4];
+            detail::throw_cuda(cudaMemcpy(v, fCols[k].p + 4 * i, sizeof(v), cudaMemcpyDeviceToHost), "cudaMemcpy");
+            p[k].set(v[0], v[1], v[2], v[3]);
+        }
+        return make(w, p, std::make_index_sequence<N>{});
+    }
+
+    struct iterator {
+        const PhaseSpaceRange* r;
+        size_t i;
+        value_type operator*() const { return (*r)[i]; }
+        value_type operator[](size_t k) const { return (*r)[i + k]; }
+        iterator& operator++() { ++i; return *this; }
+        iterator operator+(size_t k) const { return iterator{r, i + k}; }
+        bool operator!=(iterator const& o) const { return i != o.i; }
+        bool operator==(iterator const& o) const { return i == o.i; }
+    };
+    iterator begin() const { return iterator{this, 0}; }
+    iterator end() const { return iterator{this, fN}; }
+
+    // device columns: weights and daughter k ({E,px,py,pz} per event)
+    const double* weights() const { return fW.p; }
+    const double* column(size_t k) const { return fCols[k].p; }
+
+private:
+    template <size_t... I>
+    static value_type make(double w, const Vector4R (&p)[N], std::index_sequence<I...>)
+    {
+        return value_type(w, p[I]...);
+    }
+
+    size_t fN;
+    detail::DeviceBuffer<double> fCols[N];
+    detail::DeviceBuffer<double> fW;
+};
+
+template <size_t N>
+PhaseSpaceRange<N> phase_space_range(Vector4R const& mother, std::array<double, N> masses, size_t seed,
+                                     size_t length = 0)
+{
+    return PhaseSpaceRange<N>(mother, masses, seed, length);
+}
 
 }  // namespace hydra
 
