@@ -45,13 +45,21 @@ k_average_tiles_f64(DevChannel ch, DevFunctor fn, uint64_t first, uint64_t n, ui
 template <int N, int ENGINE>
 __global__ void __launch_bounds__(kAvgThreads)
 k_average_tiles_f32fix(DevChannel chd, DevChannelF ch, DevFunctor fn, uint64_t first, uint64_t n,
-                       uint64_t ntiles, hps_stats* __restrict__ partials)
+                       uint64_t ntiles, hps_stats* __restrict__ partials, const float* __restrict__ k0)
 {
-    __shared__ __align__(16) unsigned char smem[WordShare<N, ENGINE, kAvgThreads>::BYTES];
+    __shared__ __align__(16) unsigned char smem[WordShare<N, ENGINE, kAvgThreads>::BYTES2];
+    const float K0 = *k0;
     for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const hps_sums r = average_tile_f32<N, ENGINE>(chd, ch, fn, first, n, t, smem);
+        const hps_sums r = average_tile_f32<N, ENGINE>(chd, ch, fn, first, n, t, K0, smem);
         if (threadIdx.x == 0) reinterpret_cast<hps_sums*>(partials)[t] = r;
     }
+}
+
+// K0 of the call into the first 4 bytes of *out (read by the tile and final kernels).
+template <int N, int ENGINE>
+__global__ void k_shift_f32(DevChannel chd, DevChannelF ch, DevFunctor fn, uint64_t first, float* __restrict__ k0)
+{
+    if (threadIdx.x == 0) *k0 = call_shift<N, ENGINE>(chd, ch, fn, first);
 }
 
 template <int N, int ENGINE>
@@ -59,7 +67,9 @@ __global__ void __launch_bounds__(kFinalThreads)
 k_average_final_f32fix(DevChannel chd, DevChannelF ch, DevFunctor fn, uint64_t first,
                        const hps_stats* __restrict__ partials, uint64_t ntiles, hps_stats* __restrict__ out)
 {
-    const hps_stats r = merge_sums<N, ENGINE>(chd, ch, fn, first, partials, ntiles);
+    // every thread reads K0 from *out before the block reduction's barriers; thread 0 writes *out after them
+    const float K0 = ntiles ? *reinterpret_cast<const float*>(out) : 0.0f;
+    const hps_stats r = merge_sums<N, ENGINE>(chd, ch, fn, first, partials, ntiles, K0);
     if (threadIdx.x == 0) *out = r;
 }
 
@@ -94,9 +104,11 @@ hps_status launch_average(const hps_channel* channel, const DevChannel& ch, cons
         if (precision == HPS_PREC_FP32_FIX) {
             DevChannelF chf;
             to_device_channel_f(channel, &chf);
+            float* k0 = reinterpret_cast<float*>(out);
 #define HPS_BODY(NN, EE)                                                                          \
+            k_shift_f32<NN, EE><<<1, 32, 0, stream>>>(ch, chf, fn, first_evt, k0);                  \
             k_average_tiles_f32fix<NN, EE><<<grid, kAvgThreads, 0, stream>>>(ch, chf, fn, first_evt, n, \
-                                                                              ntiles, partials);
+                                                                              ntiles, partials, k0);
             HPS_DISPATCH_N_ENGINE(channel->n_daughters, channel->engine, HPS_BODY)
 #undef HPS_BODY
         } else {

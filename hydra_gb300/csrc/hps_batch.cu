@@ -45,7 +45,7 @@ struct BatchHeader {
 };
 
 // Largest shared-memory word exchange over N and engines (Philox, N = 10).
-constexpr int kBatchSmem = WordShare<10, kPhilox, kTileThreads>::BYTES;
+constexpr int kBatchSmem = WordShare<10, kPhilox, kTileThreads>::BYTES2;
 
 template <int N, int ENGINE>
 __device__ __forceinline__ void run_unit(const BatchItemDev& it, uint64_t u, int store_tile, hps_stats* partials,
@@ -54,11 +54,14 @@ __device__ __forceinline__ void run_unit(const BatchItemDev& it, uint64_t u, int
     if (it.mode == HPS_MODE_STORE) {
         const uint64_t lo = u * (uint64_t)store_tile;
         const uint64_t hi = (lo + store_tile < it.n) ? lo + store_tile : it.n;
-        for (uint64_t cb = lo; cb < hi; cb += kTileThreads)
+        // the unit fetch ends with a __syncthreads, so each unit may start at parity 0
+        int parity = 0;
+        for (uint64_t cb = lo; cb < hi; cb += kTileThreads, parity ^= 1)
             store_chunk_f32<N, ENGINE>(it.chd, it.chf, it.cols, it.weights, it.flags, it.ukey, it.first, hi, cb,
-                                       it.vec32 != 0, smem);
+                                       it.vec32 != 0, smem, parity);
     } else {
-        const hps_sums r = average_tile_f32<N, ENGINE>(it.chd, it.chf, it.fn, it.first, it.n, u, smem);
+        const float K0 = *reinterpret_cast<const float*>(it.stats);      // written by k_batch_shift
+        const hps_sums r = average_tile_f32<N, ENGINE>(it.chd, it.chf, it.fn, it.first, it.n, u, K0, smem);
         if (threadIdx.x == 0) reinterpret_cast<hps_sums*>(partials)[it.partial_offset + u] = r;
     }
 }
@@ -101,6 +104,26 @@ k_batch_f32(const BatchItemDev* __restrict__ items, BatchHeader* __restrict__ hd
     }
 }
 
+// One CTA per item slot: the shift K0 of each AverageOn item into the first 4 bytes of its stats
+// output, as k_shift_f32 does for hps_average_on.
+__global__ void k_batch_shift(const BatchItemDev* __restrict__ items, const BatchHeader* __restrict__ hdr)
+{
+    if ((int)blockIdx.x >= hdr->n_items || threadIdx.x != 0) return;
+    const BatchItemDev& it = items[blockIdx.x];
+    if (it.mode != HPS_MODE_AVERAGE || it.n == 0) return;
+    float K0 = 0.0f;
+    switch (it.N * 2 + it.engine) {
+#define HPS_SHIFT(NN)                                                                          \
+    case NN * 2 + 0: K0 = call_shift<NN, kPhilox>(it.chd, it.chf, it.fn, it.first); break;     \
+    case NN * 2 + 1: K0 = call_shift<NN, kSquares3>(it.chd, it.chf, it.fn, it.first); break;
+    HPS_SHIFT(2) HPS_SHIFT(3) HPS_SHIFT(4) HPS_SHIFT(5) HPS_SHIFT(6) HPS_SHIFT(7) HPS_SHIFT(8) HPS_SHIFT(9)
+    HPS_SHIFT(10)
+#undef HPS_SHIFT
+    default: break;
+    }
+    *reinterpret_cast<float*>(it.stats) = K0;
+}
+
 // One CTA per item slot: AverageOn items add their tile sums exactly as hps_average_on does.
 __global__ void __launch_bounds__(kFinalThreads)
 k_batch_merge(const BatchItemDev* __restrict__ items, const BatchHeader* __restrict__ hdr,
@@ -109,13 +132,15 @@ k_batch_merge(const BatchItemDev* __restrict__ items, const BatchHeader* __restr
     if ((int)blockIdx.x >= hdr->n_items) return;
     const BatchItemDev& it = items[blockIdx.x];
     if (it.mode != HPS_MODE_AVERAGE) return;
+    // every thread reads K0 before the block reduction's barriers; thread 0 writes the stats after them
+    const float K0 = it.units ? *reinterpret_cast<const float*>(it.stats) : 0.0f;
     hps_stats r{0.0, 0.0, 0.0};
     switch (it.N * 2 + it.engine) {
 #define HPS_MERGE(NN)                                                                                        \
     case NN * 2 + 0: r = merge_sums<NN, kPhilox>(it.chd, it.chf, it.fn, it.first, partials + it.partial_offset,  \
-                                                 it.units); break;                                            \
+                                                 it.units, K0); break;                                        \
     case NN * 2 + 1: r = merge_sums<NN, kSquares3>(it.chd, it.chf, it.fn, it.first,                            \
-                                                   partials + it.partial_offset, it.units); break;
+                                                   partials + it.partial_offset, it.units, K0); break;
     HPS_MERGE(2) HPS_MERGE(3) HPS_MERGE(4) HPS_MERGE(5) HPS_MERGE(6) HPS_MERGE(7) HPS_MERGE(8) HPS_MERGE(9)
     HPS_MERGE(10)
 #undef HPS_MERGE
@@ -171,6 +196,7 @@ hps_status build_graph(hps_batch_plan* p)
     cudaError_t e = cudaStreamBeginCapture(p->capture, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return cuda_status(e, "cudaStreamBeginCapture");
     cudaMemsetAsync(&p->d_header->counter, 0, sizeof(unsigned long long), p->capture);
+    k_batch_shift<<<static_cast<unsigned>(p->max_items), 32, 0, p->capture>>>(p->d_items, p->d_header);
     k_batch_f32<<<grid, kTileThreads, 0, p->capture>>>(p->d_items, p->d_header, p->d_partials);
     k_batch_merge<<<static_cast<unsigned>(p->max_items), kFinalThreads, 0, p->capture>>>(p->d_items, p->d_header,
                                                                                          p->d_partials);

@@ -46,10 +46,11 @@ __global__ void __launch_bounds__(kGenThreads)
 k_generate_f32fix(DevChannel chd, DevChannelF ch, Cols cols, double* __restrict__ weights,
                   uint8_t* __restrict__ flags, uint64_t ukey, uint64_t first, uint64_t n, int vec32)
 {
-    __shared__ __align__(16) unsigned char smem[WordShare<N, ENGINE, kGenThreads>::BYTES];
+    __shared__ __align__(16) unsigned char smem[WordShare<N, ENGINE, kGenThreads>::BYTES2];
     const uint64_t step = (uint64_t)gridDim.x * kGenThreads;
-    for (uint64_t cb = (uint64_t)blockIdx.x * kGenThreads; cb < n; cb += step)
-        store_chunk_f32<N, ENGINE>(chd, ch, cols, weights, flags, ukey, first, n, cb, vec32 != 0, smem);
+    int parity = 0;
+    for (uint64_t cb = (uint64_t)blockIdx.x * kGenThreads; cb < n; cb += step, parity ^= 1)
+        store_chunk_f32<N, ENGINE>(chd, ch, cols, weights, flags, ukey, first, n, cb, vec32 != 0, smem, parity);
 }
 
 constexpr int kMaxFunctors = 8;
@@ -75,11 +76,12 @@ __global__ void __launch_bounds__(kGenThreads)
 k_evaluate_f32fix(DevChannel chd, DevChannelF ch, Functors fs, int nf, double* __restrict__ weights,
                   OutCols out, uint64_t first, uint64_t n)
 {
-    __shared__ __align__(16) unsigned char smem[WordShare<N, ENGINE, kGenThreads>::BYTES];
+    __shared__ __align__(16) unsigned char smem[WordShare<N, ENGINE, kGenThreads>::BYTES2];
     const uint64_t step = (uint64_t)gridDim.x * kGenThreads;
-    for (uint64_t cb = (uint64_t)blockIdx.x * kGenThreads; cb < n; cb += step) {
+    int parity = 0;
+    for (uint64_t cb = (uint64_t)blockIdx.x * kGenThreads; cb < n; cb += step, parity ^= 1) {
         uint64_t w[3 * N - 4];
-        cta_event_words<N, ENGINE, kGenThreads>(chd.key, first + cb, smem, w);
+        cta_event_words<N, ENGINE, kGenThreads>(chd.key, first + cb, smem, w, parity);
         const uint64_t e = cb + threadIdx.x;
         if (e < n) {
             float p[N][4];

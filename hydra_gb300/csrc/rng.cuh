@@ -179,16 +179,23 @@ template <int N, int ENGINE, int NT> struct WordShare {
     static constexpr int B = (ENGINE == kPhilox) ? (NW + 1) / 2 : NW;   // items per event
     static constexpr int SLOTS = NT + B - 1;
     static constexpr int BYTES = SLOTS * ((ENGINE == kPhilox) ? 16 : 8);
+    static constexpr int BYTES2 = 2 * BYTES;                            // two buffers, see below
 };
 
-// All NT threads of the CTA must call together; e0 = event of thread 0.  Near the end of the
-// 2^64 counter range the Philox carry into the high counter word differs between neighbouring
-// events, so there each thread computes its own blocks (a CTA-uniform branch).
+// All NT threads of the CTA must call together; e0 = event of thread 0.  smem holds two buffers
+// (WordShare::BYTES2) and `parity` picks one: a call writes its buffer, waits at one barrier, and
+// reads it back.  Consecutive calls alternate the parity, so the next call's writes go to the
+// other buffer, and the barrier of that call keeps the writes of the call after it away from this
+// one's reads; a call that repeats the previous call's parity must follow a __syncthreads.  Near
+// the end of the 2^64 counter range the Philox carry into the high counter word differs between
+// neighbouring events, so there each thread computes its own blocks (a CTA-uniform branch).
 template <int N, int ENGINE, int NT>
-__device__ __forceinline__ void cta_event_words(uint64_t key, uint64_t e0, void* smem, uint64_t (&w)[3 * N - 4])
+__device__ __forceinline__ void cta_event_words(uint64_t key, uint64_t e0, void* smem, uint64_t (&w)[3 * N - 4],
+                                                int parity)
 {
     using S = WordShare<N, ENGINE, NT>;
     const int t = threadIdx.x;
+    smem = static_cast<unsigned char*>(smem) + (parity & 1) * S::BYTES;
     if constexpr (ENGINE == kPhilox) {
         ulonglong2* slots = static_cast<ulonglong2*>(smem);
         const uint64_t c_first = e0 + 3u * N + 1u;                 // counter of slot 0
@@ -210,7 +217,6 @@ __device__ __forceinline__ void cta_event_words(uint64_t key, uint64_t e0, void*
                 w[2 * b] = v.x;
                 if (2 * b + 1 < S::NW) w[2 * b + 1] = v.y;
             }
-            __syncthreads();
         } else {
             event_words<N, kPhilox>(key, e0 + t, w);
         }
@@ -222,7 +228,6 @@ __device__ __forceinline__ void cta_event_words(uint64_t key, uint64_t e0, void*
         __syncthreads();
 #pragma unroll
         for (int k = 0; k < S::NW; ++k) w[k] = slots[t + k];
-        __syncthreads();
     }
 }
 

@@ -17,15 +17,16 @@ constexpr int kAvgPerThread = HPS_AVG_TILE / kTileThreads;
 static_assert(kTileThreads * kAvgPerThread == HPS_AVG_TILE, "tile shape");
 constexpr int kFinalThreads = 1024;
 
-// Events [cb, cb + NT) of the call (event index first + e); all NT threads call together.
+// Events [cb, cb + NT) of the call (event index first + e); all NT threads call together, with
+// the word-buffer parity alternating between consecutive calls (cta_event_words).
 template <int N, int ENGINE>
 __device__ __forceinline__ void store_chunk_f32(const DevChannel& chd, const DevChannelF& ch, const Cols& cols,
                                                 double* __restrict__ weights, uint8_t* __restrict__ flags,
                                                 uint64_t ukey, uint64_t first, uint64_t n, uint64_t cb,
-                                                bool vec32, void* smem)
+                                                bool vec32, void* smem, int parity)
 {
     uint64_t w[3 * N - 4];
-    cta_event_words<N, ENGINE, kTileThreads>(chd.key, first + cb, smem, w);
+    cta_event_words<N, ENGINE, kTileThreads>(chd.key, first + cb, smem, w, parity);
     const uint64_t e = cb + threadIdx.x;
     if (e < n) {
         float p[N][4];
@@ -94,24 +95,18 @@ __device__ __forceinline__ hps_sums block_reduce_sums(hps_sums s)
     return s;
 }
 
-// The shift K0: the functor value of the call's first event, computed by thread 0 and handed
-// to every thread of the CTA.
+// The shift K0: the functor value of the call's first event.  One thread computes it once per
+// call (k_shift_f32 / k_batch_shift) into the first 4 bytes of the call's hps_stats output, which
+// the tile and merge kernels read before the merge overwrites it with the result.
 template <int N, int ENGINE>
-__device__ __forceinline__ float shift_value(const DevChannel& chd, const DevChannelF& ch, const DevFunctor& fn,
-                                             uint64_t first)
+__device__ __forceinline__ float call_shift(const DevChannel& chd, const DevChannelF& ch, const DevFunctor& fn,
+                                            uint64_t first)
 {
-    __shared__ float s_k0;
-    if (threadIdx.x == 0) {
-        uint64_t w[3 * N - 4];
-        event_words<N, ENGINE>(chd.key, first, w);
-        float p[N][4];
-        f32::event_from_words<N, ENGINE>(chd, ch, w, p);
-        s_k0 = f32::functor<N>(fn, p);
-    }
-    __syncthreads();
-    const float k0 = s_k0;
-    __syncthreads();
-    return k0;
+    uint64_t w[3 * N - 4];
+    event_words<N, ENGINE>(chd.key, first, w);
+    float p[N][4];
+    f32::event_from_words<N, ENGINE>(chd, ch, w, p);
+    return f32::functor<N>(fn, p);
 }
 
 // AverageOn tile t: thread j takes events t*4096 + j + 256k, k = 0..15, and accumulates their
@@ -121,16 +116,15 @@ __device__ __forceinline__ float shift_value(const DevChannel& chd, const DevCha
 template <int N, int ENGINE>
 __device__ __forceinline__ hps_sums average_tile_f32(const DevChannel& chd, const DevChannelF& ch,
                                                      const DevFunctor& fn, uint64_t first, uint64_t n,
-                                                     uint64_t t, void* smem)
+                                                     uint64_t t, float K0, void* smem)
 {
-    const float K0 = shift_value<N, ENGINE>(chd, ch, fn, first);
     float swh = 0.0f, swl = 0.0f, s1h = 0.0f, s1l = 0.0f, s2h = 0.0f, s2l = 0.0f;
     const uint64_t base = t * HPS_AVG_TILE;
     for (int k = 0; k < kAvgPerThread; ++k) {
         const uint64_t cb = base + (uint64_t)k * kTileThreads;
         if (cb >= n) break;                                              // CTA-uniform
         uint64_t w[3 * N - 4];
-        cta_event_words<N, ENGINE, kTileThreads>(chd.key, first + cb, smem, w);
+        cta_event_words<N, ENGINE, kTileThreads>(chd.key, first + cb, smem, w, k);
         const uint64_t e = cb + threadIdx.x;
         if (e < n) {
             float p[N][4];
@@ -158,7 +152,7 @@ __device__ __forceinline__ hps_sums average_tile_f32(const DevChannel& chd, cons
 template <int N, int ENGINE>
 __device__ __forceinline__ hps_stats merge_sums(const DevChannel& chd, const DevChannelF& ch, const DevFunctor& fn,
                                                 uint64_t first, const hps_stats* __restrict__ partials,
-                                                uint64_t ntiles)
+                                                uint64_t ntiles, float K0)
 {
     const hps_sums* tiles = reinterpret_cast<const hps_sums*>(partials);
     hps_sums acc{0.0, 0.0, 0.0};
@@ -167,7 +161,6 @@ __device__ __forceinline__ hps_stats merge_sums(const DevChannel& chd, const Dev
         acc.s1 += v.s1; acc.s2 += v.s2; acc.w += v.w;
     }
     const hps_sums tot = block_reduce_sums<kFinalThreads>(acc);
-    const float K0 = (ntiles > 0) ? shift_value<N, ENGINE>(chd, ch, fn, first) : 0.0f;
     hps_stats r{0.0, 0.0, 0.0};
     if (tot.w != 0.0) {
         const double q = tot.s1 / tot.w;
