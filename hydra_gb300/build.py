@@ -73,7 +73,8 @@ def build(verbose: bool = False, force: bool = False) -> Path:
                     sys.stderr.write(r.stdout + r.stderr)
                 if r.returncode != 0:
                     raise RuntimeError(f"nvcc failed on {src.name}")
-    if jobs or not LIB.exists():
+    # relink whenever an object is newer than the library (a failed link leaves the old one behind)
+    if jobs or not LIB.exists() or any(o.stat().st_mtime > LIB.stat().st_mtime for o in objs):
         tmp = LIB.with_suffix(f".{os.getpid()}.tmp")
         r = subprocess.run([cc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"],
                            capture_output=True, text=True)

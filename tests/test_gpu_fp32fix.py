@@ -124,3 +124,14 @@ def test_fp32fix_average_on(api, torch, oracle, name, N, engine, M, masses):
     out2 = torch.zeros(3, dtype=torch.float64, device="cuda")
     api.average_on(ch, 0, n, fn, out2, None, precision="fp32_fix")
     assert out2.cpu().tolist() == [mean, m2, W]
+
+
+def test_fp32fix_near_coincident_uniforms(api, torch, oracle):
+    """Events 21689203-21689204 of the N=10 config-3 channel (Philox seed 0x3039) have two sorted
+    uniforms only 1.4e-11 apart, so one stage sits 5e-11 GeV above threshold.  The reference's
+    uniforms are double(word) / 2^64; the gap must be taken between those rounded values (the exact
+    word difference differs from it by 4e-6 relative here).  The FP64 reference itself loses about
+    2.5e-7 to the cancellation in a - b - c on such a stage (tests/test_oracle_exact.py)."""
+    e4, ew, _, _, _ = errors(api, torch, oracle, 10, 0, 5.0, [PI] * 10, 4, first=21689202)
+    print(f"\n[fp32_fix] near-coincident uniforms: four {e4:.3e}, weight {ew:.3e}")
+    assert e4 <= TOL and ew <= TOL
