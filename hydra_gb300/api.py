@@ -171,6 +171,19 @@ def average_on(ch: HpsChannel, first: int, n: int, functor: HpsFunctor, out: tor
                                wbytes, _PRECISIONS[precision], _stream_handle(stream)))
 
 
+def generate_average(ch: HpsChannel, first: int, four: torch.Tensor, weights, flags, functor: HpsFunctor,
+                     out: torch.Tensor, workspace: torch.Tensor | None = None,
+                     unweight_seed: int = DEFAULT_UNWEIGHT_SEED, precision="fp64", stream=None) -> None:
+    """Generate (into four [N, n, 4], weights, flags) and AverageOn (into out {mean, M2, W}) of the
+    same events in one pass; each result equals its separate call bit for bit."""
+    N, n = four.shape[0], four.shape[1]
+    arr = _ptr_array([four[k] for k in range(N)])
+    wbytes = 0 if workspace is None else workspace.numel() * workspace.element_size()
+    check(lib().hps_generate_average(ctypes.byref(ch), first, n, ctypes.cast(arr, ctypes.c_void_p), _dptr(weights),
+                                     _dptr(flags), unweight_seed & (2**64 - 1), ctypes.byref(functor), _dptr(out),
+                                     _dptr(workspace), wbytes, _PRECISIONS[precision], _stream_handle(stream)))
+
+
 def generate_mothers(ch: HpsChannel, first: int, mothers: torch.Tensor, four: torch.Tensor, weights=None,
                      precision="fp64", stream=None) -> None:
     """DecayMothers: mothers [n, 4] (a Vector4R column), four [N, n, 4]."""

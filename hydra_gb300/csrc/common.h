@@ -32,9 +32,11 @@ void to_device_channel_f(const hps_channel* ch, DevChannelF* out);
 // touches no device state, and the tile + final-merge launches into caller-provided partials.
 hps_status average_args(const hps_channel* channel, const hps_functor* functor, int32_t precision,
                         DevChannel* ch, DevFunctor* fn);
+// With `so`, the tiles also store their events (hps_generate_average).
+struct StoreOut;
 hps_status launch_average(const hps_channel* channel, const DevChannel& ch, const DevFunctor& fn,
                           uint64_t first_evt, uint64_t n, hps_stats* out, hps_stats* partials,
-                          int32_t precision, cudaStream_t stream);
+                          int32_t precision, cudaStream_t stream, const StoreOut* so = nullptr);
 
 // Stored events: N daughter columns of Vector4R (32 bytes per event, 16-byte aligned).
 struct ConstCols { const double* p[HPS_MAX_DAUGHTERS]; };

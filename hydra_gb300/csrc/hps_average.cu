@@ -41,6 +41,40 @@ k_average_tiles_f64(DevChannel ch, DevFunctor fn, uint64_t first, uint64_t n, ui
     }
 }
 
+// Generate + AverageOn of the same events in one pass, FP64 form: the tile fold above with every
+// event also stored as k_generate_f64 stores it (four-vectors, weight, FlagDaugthers flag).
+template <int N, int ENGINE>
+__global__ void __launch_bounds__(kAvgThreads)
+k_generate_average_f64(DevChannel ch, DevFunctor fn, uint64_t first, uint64_t n, uint64_t ntiles,
+                       hps_stats* __restrict__ partials, StoreOut so)
+{
+    for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        hps_stats acc{0.0, 0.0, 0.0};
+        const uint64_t base = t * HPS_AVG_TILE + threadIdx.x;
+        for (int k = 0; k < kAvgPerThread; ++k) {
+            const uint64_t e = base + (uint64_t)k * kAvgThreads;
+            if (e < n) {
+                double p[N][4];
+                hps_stats y;
+                y.w = f64::event<N, ENGINE>(ch, first + e, p);
+#pragma unroll
+                for (int d = 0; d < N; ++d) store_vec4(so.cols.p[d], e, p[d], so.vec32 != 0);
+                if (so.weights) so.weights[e] = y.w;
+                if (so.flags) {
+                    const double wr = f64::recomputed_weight<N>(ch.masses, ch.max_weight, p);
+                    const double u = static_cast<double>(squares3_word(so.ukey, first + e)) * 0x1p-32;
+                    so.flags[e] = (f64::dvd(wr, ch.max_weight) > u) ? 1 : 0;
+                }
+                y.mean = functor_f64<N>(fn, p);
+                y.m2 = 0.0;
+                acc = stats_merge(acc, y);
+            }
+        }
+        const hps_stats r = block_reduce_stats<kAvgThreads>(acc);
+        if (threadIdx.x == 0) partials[t] = r;
+    }
+}
+
 // FP32_FIX form: average_tile_f32 (tiles_f32.cuh) per tile, CTA-shared random words.
 template <int N, int ENGINE>
 __global__ void __launch_bounds__(kAvgThreads)
@@ -51,6 +85,20 @@ k_average_tiles_f32fix(DevChannel chd, DevChannelF ch, DevFunctor fn, uint64_t f
     const float K0 = *k0;
     for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const hps_sums r = average_tile_f32<N, ENGINE>(chd, ch, fn, first, n, t, K0, smem);
+        if (threadIdx.x == 0) reinterpret_cast<hps_sums*>(partials)[t] = r;
+    }
+}
+
+template <int N, int ENGINE>
+__global__ void __launch_bounds__(kAvgThreads)
+k_generate_average_f32fix(DevChannel chd, DevChannelF ch, DevFunctor fn, uint64_t first, uint64_t n,
+                          uint64_t ntiles, hps_stats* __restrict__ partials, const float* __restrict__ k0,
+                          StoreOut so)
+{
+    __shared__ __align__(16) unsigned char smem[WordShare<N, ENGINE, kAvgThreads>::BYTES2];
+    const float K0 = *k0;
+    for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const hps_sums r = average_tile_f32<N, ENGINE, true>(chd, ch, fn, first, n, t, K0, smem, &so);
         if (threadIdx.x == 0) reinterpret_cast<hps_sums*>(partials)[t] = r;
     }
 }
@@ -96,7 +144,7 @@ hps_status average_args(const hps_channel* channel, const hps_functor* functor, 
 
 hps_status launch_average(const hps_channel* channel, const DevChannel& ch, const DevFunctor& fn,
                           uint64_t first_evt, uint64_t n, hps_stats* out, hps_stats* partials,
-                          int32_t precision, cudaStream_t stream)
+                          int32_t precision, cudaStream_t stream, const StoreOut* so)
 {
     const uint64_t ntiles = (n + HPS_AVG_TILE - 1) / HPS_AVG_TILE;
     if (ntiles > 0) {
@@ -107,14 +155,22 @@ hps_status launch_average(const hps_channel* channel, const DevChannel& ch, cons
             float* k0 = reinterpret_cast<float*>(out);
 #define HPS_BODY(NN, EE)                                                                          \
             k_shift_f32<NN, EE><<<1, 32, 0, stream>>>(ch, chf, fn, first_evt, k0);                  \
-            k_average_tiles_f32fix<NN, EE><<<grid, kAvgThreads, 0, stream>>>(ch, chf, fn, first_evt, n, \
-                                                                              ntiles, partials, k0);
+            if (so)                                                                                \
+                k_generate_average_f32fix<NN, EE><<<grid, kAvgThreads, 0, stream>>>(               \
+                    ch, chf, fn, first_evt, n, ntiles, partials, k0, *so);                         \
+            else                                                                                   \
+                k_average_tiles_f32fix<NN, EE><<<grid, kAvgThreads, 0, stream>>>(ch, chf, fn, first_evt, n, \
+                                                                                  ntiles, partials, k0);
             HPS_DISPATCH_N_ENGINE(channel->n_daughters, channel->engine, HPS_BODY)
 #undef HPS_BODY
         } else {
 #define HPS_BODY(NN, EE)                                                                          \
-            k_average_tiles_f64<NN, EE><<<grid, kAvgThreads, 0, stream>>>(ch, fn, first_evt, n, ntiles, \
-                                                                           partials);
+            if (so)                                                                                \
+                k_generate_average_f64<NN, EE><<<grid, kAvgThreads, 0, stream>>>(ch, fn, first_evt, n, \
+                                                                                  ntiles, partials, *so); \
+            else                                                                                   \
+                k_average_tiles_f64<NN, EE><<<grid, kAvgThreads, 0, stream>>>(ch, fn, first_evt, n, ntiles, \
+                                                                               partials);
             HPS_DISPATCH_N_ENGINE(channel->n_daughters, channel->engine, HPS_BODY)
 #undef HPS_BODY
         }
@@ -170,6 +226,56 @@ hps_status hps_average_on(const hps_channel* channel, uint64_t first_evt, uint64
         return set_error(HPS_ERR_OOM, "cudaMallocAsync(%zu): %s", need, cudaGetErrorString(e));
     }
     st = launch_average(channel, ch, fn, first_evt, n, out, static_cast<hps_stats*>(scratch), precision, s);
+    e = cudaFreeAsync(scratch, s);
+    if (st == HPS_OK && e != cudaSuccess) return cuda_status(e, "cudaFreeAsync");
+    return st;
+}
+
+hps_status hps_generate_average(const hps_channel* channel, uint64_t first_evt, uint64_t n, double* const* cols,
+                                double* weights, uint8_t* flags, uint64_t unweight_seed, const hps_functor* functor,
+                                hps_stats* out, void* workspace, size_t workspace_bytes, int32_t precision,
+                                void* stream)
+{
+    clear_error();
+    DevChannel ch;
+    DevFunctor fn;
+    hps_status st = average_args(channel, functor, precision, &ch, &fn);
+    if (st != HPS_OK) return st;
+    if (!out || !aligned(out, 8)) return set_error(HPS_ERR_BAD_ARG, "out NULL or not 8-byte aligned");
+    if (!range_ok(first_evt, n)) return set_error(HPS_ERR_BAD_ARG, "event range wraps 2^64");
+    StoreOut so{};
+    const int N = channel->n_daughters;
+    if (n) {
+        if (!cols) return set_error(HPS_ERR_BAD_ARG, "cols is NULL");
+        bool all32 = true;
+        for (int k = 0; k < N; ++k) {
+            if (!cols[k]) return set_error(HPS_ERR_BAD_ARG, "column %d is NULL", k);
+            if (!aligned(cols[k], 16)) return set_error(HPS_ERR_BAD_ARG, "column %d not 16-byte aligned", k);
+            all32 = all32 && aligned(cols[k], 32);
+            so.cols.p[k] = cols[k];
+        }
+        so.vec32 = all32 ? 1 : 0;
+    }
+    if (weights && !aligned(weights, 8)) return set_error(HPS_ERR_BAD_ARG, "weights not 8-byte aligned");
+    so.weights = weights;
+    so.flags = flags;
+    so.ukey = splitmix64(unweight_seed);
+    const size_t need = hps_average_on_workspace_size(n);
+    cudaStream_t s = as_stream(stream);
+    if (workspace) {
+        if (workspace_bytes < need)
+            return set_error(HPS_ERR_BAD_ARG, "workspace of %zu bytes, %zu needed", workspace_bytes, need);
+        if (!aligned(workspace, 8)) return set_error(HPS_ERR_BAD_ARG, "workspace not 8-byte aligned");
+        return launch_average(channel, ch, fn, first_evt, n, out, static_cast<hps_stats*>(workspace), precision, s,
+                              &so);
+    }
+    void* scratch = nullptr;
+    cudaError_t e = cudaMallocAsync(&scratch, need, s);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(HPS_ERR_OOM, "cudaMallocAsync(%zu): %s", need, cudaGetErrorString(e));
+    }
+    st = launch_average(channel, ch, fn, first_evt, n, out, static_cast<hps_stats*>(scratch), precision, s, &so);
     e = cudaFreeAsync(scratch, s);
     if (st == HPS_OK && e != cudaSuccess) return cuda_status(e, "cudaFreeAsync");
     return st;

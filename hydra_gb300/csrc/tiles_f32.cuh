@@ -17,6 +17,31 @@ constexpr int kAvgPerThread = HPS_AVG_TILE / kTileThreads;
 static_assert(kTileThreads * kAvgPerThread == HPS_AVG_TILE, "tile shape");
 constexpr int kFinalThreads = 1024;
 
+// Where a storing work unit puts event e of the call: Decays columns, weight, unweight flag.
+struct StoreOut {
+    Cols cols;
+    double* weights;      // may be NULL
+    uint8_t* flags;       // may be NULL
+    uint64_t ukey;        // splitmix64 of the unweight seed
+    int vec32;            // all columns 32-byte aligned
+};
+
+template <int N>
+__device__ __forceinline__ void store_event_f32(const float (&p)[N][4], const f32::EventWeight& ew,
+                                                const Cols& cols, double* __restrict__ weights,
+                                                uint8_t* __restrict__ flags, uint64_t ukey, uint64_t first,
+                                                uint64_t e, bool vec32)
+{
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        const double v[4] = {f32::widen_pos(p[k][0]), f32::widen(p[k][1]), f32::widen(p[k][2]),
+                             f32::widen(p[k][3])};
+        store_vec4(cols.p[k], e, v, vec32);
+    }
+    if (weights) weights[e] = ew.weight;
+    if (flags) flags[e] = f32::accept(ew, squares3_word(ukey, first + e)) ? 1 : 0;
+}
+
 // Events [cb, cb + NT) of the call (event index first + e); all NT threads call together, with
 // the word-buffer parity alternating between consecutive calls (cta_event_words).
 template <int N, int ENGINE>
@@ -31,14 +56,7 @@ __device__ __forceinline__ void store_chunk_f32(const DevChannel& chd, const Dev
     if (e < n) {
         float p[N][4];
         const f32::EventWeight ew = f32::event_from_words<N, ENGINE>(chd, ch, w, p);
-#pragma unroll
-        for (int k = 0; k < N; ++k) {
-            const double v[4] = {f32::widen_pos(p[k][0]), f32::widen(p[k][1]), f32::widen(p[k][2]),
-                                 f32::widen(p[k][3])};
-            store_vec4(cols.p[k], e, v, vec32);
-        }
-        if (weights) weights[e] = ew.weight;
-        if (flags) flags[e] = f32::accept(ew, squares3_word(ukey, first + e)) ? 1 : 0;
+        store_event_f32<N>(p, ew, cols, weights, flags, ukey, first, e, vec32);
     }
 }
 
@@ -112,11 +130,14 @@ __device__ __forceinline__ float call_shift(const DevChannel& chd, const DevChan
 // AverageOn tile t: thread j takes events t*4096 + j + 256k, k = 0..15, and accumulates their
 // prod(pdk) P (the weight without the common factor max_weight) as float-float sums
 // sum P, sum P (f - K0), sum P (f - K0)^2, converted to double and scaled by max_weight; the
-// fixed CTA tree adds the per-thread sums.  Result valid in thread 0.
-template <int N, int ENGINE>
+// fixed CTA tree adds the per-thread sums.  Result valid in thread 0.  With STORE, every event is
+// also stored (Generate and AverageOn of the same events in one pass): the sums are those of the
+// plain tile, bit for bit, and the stored events those of store_chunk_f32.
+template <int N, int ENGINE, bool STORE = false>
 __device__ __forceinline__ hps_sums average_tile_f32(const DevChannel& chd, const DevChannelF& ch,
                                                      const DevFunctor& fn, uint64_t first, uint64_t n,
-                                                     uint64_t t, float K0, void* smem)
+                                                     uint64_t t, float K0, void* smem,
+                                                     const StoreOut* so = nullptr)
 {
     float swh = 0.0f, swl = 0.0f, s1h = 0.0f, s1l = 0.0f, s2h = 0.0f, s2l = 0.0f;
     const uint64_t base = t * HPS_AVG_TILE;
@@ -129,6 +150,8 @@ __device__ __forceinline__ hps_sums average_tile_f32(const DevChannel& chd, cons
         if (e < n) {
             float p[N][4];
             const f32::EventWeight ew = f32::event_from_words<N, ENGINE>(chd, ch, w, p);
+            if constexpr (STORE)
+                store_event_f32<N>(p, ew, so->cols, so->weights, so->flags, so->ukey, first, e, so->vec32 != 0);
             const float d = f32::functor<N>(fn, p) - K0;
             // P*d and P*d^2 as float-float products
             const float h1 = ew.prod_hi * d;

@@ -177,6 +177,17 @@ hps_status hps_average_on(const hps_channel* ch, uint64_t first_evt, uint64_t n,
                           const hps_functor* functor, hps_stats* out, void* workspace,
                           size_t workspace_bytes, int32_t precision, void* stream);
 
+/* Generate and AverageOn of the same events in one pass: the reference needs two calls,
+ * PhaseSpace::Generate(mother, events) and AverageOn(policy, mother, functor, n)
+ * (PhaseSpace.inl:255-273, 377-394), which each generate events [first_evt, first_evt + n).
+ * The stored events, weights and flags equal those of hps_generate, and *out equals the
+ * hps_average_on result, bit for bit (same tiles, same order); the event body runs once instead
+ * of twice.  Arguments as in hps_generate and hps_average_on. */
+hps_status hps_generate_average(const hps_channel* ch, uint64_t first_evt, uint64_t n, double* const* cols,
+                                double* weights, uint8_t* flags, uint64_t unweight_seed,
+                                const hps_functor* functor, hps_stats* out, void* workspace,
+                                size_t workspace_bytes, int32_t precision, void* stream);
+
 /* AverageOn that makes no device allocation at all (no counterpart in the reference; Hydra's
  * own reduction always takes temporary storage from its allocator).  It is meant for host
  * programs that may not allocate device memory once they are running -- for example a
