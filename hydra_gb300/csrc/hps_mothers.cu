@@ -10,6 +10,7 @@
 // with hash(evt, seed), no discard) and takes ECM and the maximum weight from the mother's mass.
 #include "common.h"
 #include "store.cuh"
+#include "tiles_f32.cuh"
 
 namespace hps {
 
@@ -17,14 +18,6 @@ struct MCols { double* p[HPS_MAX_DAUGHTERS]; };
 constexpr int kMaxMotherFunctors = 8;
 struct MFunctors { DevFunctor f[kMaxMotherFunctors]; };
 struct MOut { double* p[kMaxMotherFunctors]; };
-
-template <int N>
-__device__ __forceinline__ void load_mother(const double* __restrict__ mothers, uint64_t e, double (&mo)[4])
-{
-    const double2 a = __ldg(reinterpret_cast<const double2*>(mothers + 4 * e));
-    const double2 b = __ldg(reinterpret_cast<const double2*>(mothers + 4 * e) + 1);
-    mo[0] = a.x; mo[1] = a.y; mo[2] = b.x; mo[3] = b.y;
-}
 
 // (mother, daughters...) as the *Mothers functors see them.
 template <int N>
@@ -113,14 +106,85 @@ k_average_mothers_final(const hps_stats* __restrict__ partials, uint64_t ntiles,
     if (threadIdx.x == 0) *out = r;
 }
 
+// FP32_FIX DecayMothers: the store path of k_generate_f32fix (CTA-shared words: the stream is the
+// DecayMother one) with each event boosted by its own mother (f32::boost_to_mother).
+template <int N, int ENGINE>
+__global__ void __launch_bounds__(kTileThreads)
+k_generate_mothers_f32fix(DevChannel chd, DevChannelF ch, const double* __restrict__ mothers, Cols cols,
+                          double* __restrict__ weights, uint64_t first, uint64_t n, int vec32)
+{
+    __shared__ __align__(16) unsigned char smem[WordShare<N, ENGINE, kTileThreads>::BYTES2];
+    const uint64_t step = (uint64_t)gridDim.x * kTileThreads;
+    int parity = 0;
+    for (uint64_t cb = (uint64_t)blockIdx.x * kTileThreads; cb < n; cb += step, parity ^= 1) {
+        uint64_t w[3 * N - 4];
+        cta_event_words<N, ENGINE, kTileThreads>(chd.key, first + cb, smem, w, parity);
+        const uint64_t e = cb + threadIdx.x;
+        if (e < n) {
+            double mo[4];
+            load_mother<N>(mothers, e, mo);
+            float p[N][4];
+            const f32::EventWeight ew = f32::event_from_words<N, ENGINE>(chd, ch, w, p);
+            f32::boost_to_mother<N>(p, ch.m2, f32::mother_frame(mo));
+            store_event_f32<N>(p, ew, cols, weights, nullptr, 0, first, e, vec32 != 0);
+        }
+    }
+}
+
+// FP32_FIX AverageMothers: the tiles of k_average_tiles_f32fix with mothers; K0 from event `first`.
+template <int N, int ENGINE>
+__global__ void k_shift_mothers_f32(DevChannel chd, DevChannelF ch, DevFunctor fn, uint64_t first,
+                                    const double* __restrict__ mothers, float* __restrict__ k0)
+{
+    if (threadIdx.x != 0) return;
+    uint64_t w[3 * N - 4];
+    event_words<N, ENGINE>(chd.key, first, w);
+    float p[N][4];
+    f32::event_from_words<N, ENGINE>(chd, ch, w, p);
+    double mo[4];
+    load_mother<N>(mothers, 0, mo);
+    const f32::MotherFrame mf = f32::mother_frame(mo);
+    f32::boost_to_mother<N>(p, ch.m2, mf);
+    *k0 = mother_functor_f32<N>(fn, mf, p);
+}
+
+template <int N, int ENGINE>
+__global__ void __launch_bounds__(kTileThreads)
+k_average_mothers_tiles_f32fix(DevChannel chd, DevChannelF ch, DevFunctor fn, uint64_t first, uint64_t n,
+                               uint64_t ntiles, hps_stats* __restrict__ partials, const float* __restrict__ k0,
+                               const double* __restrict__ mothers)
+{
+    __shared__ __align__(16) unsigned char smem[WordShare<N, ENGINE, kTileThreads>::BYTES2];
+    const float K0 = *k0;
+    for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const hps_sums r = average_tile_f32<N, ENGINE, false, true>(chd, ch, fn, first, n, t, K0, smem, nullptr,
+                                                                   mothers);
+        if (threadIdx.x == 0) reinterpret_cast<hps_sums*>(partials)[t] = r;
+    }
+}
+
+template <int N, int ENGINE>
+__global__ void __launch_bounds__(kFinalThreads)
+k_average_mothers_final_f32fix(DevChannel chd, DevChannelF ch, DevFunctor fn, uint64_t first,
+                               const hps_stats* __restrict__ partials, uint64_t ntiles, hps_stats* __restrict__ out)
+{
+    // every thread reads K0 from *out before the block reduction's barriers; thread 0 writes *out after them
+    const float K0 = ntiles ? *reinterpret_cast<const float*>(out) : 0.0f;
+    const hps_stats r = merge_sums<N, ENGINE>(chd, ch, fn, first, partials, ntiles, K0);
+    if (threadIdx.x == 0) *out = r;
+}
+
 static hps_status mother_args(const hps_channel* channel, uint64_t first, uint64_t n, const double* mothers,
-                              int32_t precision, DevChannel* ch)
+                              int32_t precision, DevChannel* ch, bool fp32_ok)
 {
     hps_status st = to_device_channel(channel, ch);
     if (st != HPS_OK) return st;
-    if (precision != HPS_PREC_FP64)
-        return set_error(precision == HPS_PREC_FP32_FIX ? HPS_ERR_UNSUPPORTED : HPS_ERR_BAD_ARG,
-                         "the per-event-mother forms are built for HPS_PREC_FP64 only");
+    ch->boost_active = 0;              // the mothers' own boosts replace the channel's
+    if (precision != HPS_PREC_FP64 && !(fp32_ok && precision == HPS_PREC_FP32_FIX)) {
+        if (precision == HPS_PREC_FP32_FIX)
+            return set_error(HPS_ERR_UNSUPPORTED, "EvalMothers is built for HPS_PREC_FP64 only");
+        return set_error(HPS_ERR_BAD_ARG, "unknown precision %d", precision);
+    }
     if (!range_ok(first, n)) return set_error(HPS_ERR_BAD_ARG, "event range wraps 2^64");
     if (n && !mothers) return set_error(HPS_ERR_BAD_ARG, "mothers is NULL");
     if (!aligned(mothers, 16)) return set_error(HPS_ERR_BAD_ARG, "mothers not 16-byte aligned");
@@ -144,7 +208,7 @@ hps_status hps_generate_mothers(const hps_channel* channel, uint64_t first_evt, 
 {
     clear_error();
     DevChannel ch;
-    hps_status st = mother_args(channel, first_evt, n, mothers, precision, &ch);
+    hps_status st = mother_args(channel, first_evt, n, mothers, precision, &ch, true);
     if (st != HPS_OK || n == 0) return st;
     if (!cols) return set_error(HPS_ERR_BAD_ARG, "cols is NULL");
     const int N = channel->n_daughters;
@@ -156,6 +220,18 @@ hps_status hps_generate_mothers(const hps_channel* channel, uint64_t first_evt, 
         cc.p[k] = cols[k];
     }
     const unsigned grid = grid_for(n, 256);
+    if (precision == HPS_PREC_FP32_FIX) {
+        DevChannelF chf;
+        to_device_channel_f(channel, &chf);
+        Cols c32{};
+        for (int k = 0; k < N; ++k) c32.p[k] = cc.p[k];
+#define HPS_BODY(NN, EE)                                                                                 \
+        k_generate_mothers_f32fix<NN, EE><<<grid, kTileThreads, 0, as_stream(stream)>>>(ch, chf, mothers, c32, \
+                                                                                     weights, first_evt, n, all32 ? 1 : 0);
+        HPS_DISPATCH_N_ENGINE(N, channel->engine, HPS_BODY)
+#undef HPS_BODY
+        return cuda_status(cudaGetLastError(), "hps_generate_mothers launch");
+    }
 #define HPS_BODY(NN, EE)                                                                                 \
     k_generate_mothers_f64<NN, EE><<<grid, 256, 0, as_stream(stream)>>>(ch, mothers, cc, weights, first_evt, n, \
                                                                          all32 ? 1 : 0);
@@ -170,7 +246,7 @@ hps_status hps_evaluate_mothers(const hps_channel* channel, uint64_t first_evt, 
 {
     clear_error();
     DevChannel ch;
-    hps_status st = mother_args(channel, first_evt, n, mothers, precision, &ch);
+    hps_status st = mother_args(channel, first_evt, n, mothers, precision, &ch, false);
     if (st != HPS_OK) return st;
     if (n_functors < 0 || n_functors > kMaxMotherFunctors)
         return set_error(HPS_ERR_BAD_ARG, "n_functors %d outside 0..%d", n_functors, kMaxMotherFunctors);
@@ -198,7 +274,7 @@ hps_status hps_average_on_mothers(const hps_channel* channel, uint64_t first_evt
 {
     clear_error();
     DevChannel ch;
-    hps_status st = mother_args(channel, first_evt, n, mothers, precision, &ch);
+    hps_status st = mother_args(channel, first_evt, n, mothers, precision, &ch, true);
     if (st != HPS_OK) return st;
     DevFunctor fn;
     if ((st = mother_functor(functor, channel->n_daughters, &fn)) != HPS_OK) return st;
@@ -220,14 +296,29 @@ hps_status hps_average_on_mothers(const hps_channel* channel, uint64_t first_evt
     }
     hps_stats* partials = static_cast<hps_stats*>(scratch);
     const uint64_t ntiles = (n + HPS_AVG_TILE - 1) / HPS_AVG_TILE;
-    if (ntiles) {
-        const unsigned grid = static_cast<unsigned>(ntiles < 152u * 16u ? ntiles : 152u * 16u);
+    const unsigned grid = static_cast<unsigned>(ntiles < 152u * 16u ? (ntiles ? ntiles : 1) : 152u * 16u);
+    if (precision == HPS_PREC_FP32_FIX) {
+        DevChannelF chf;
+        to_device_channel_f(channel, &chf);
+        float* k0 = reinterpret_cast<float*>(out);
 #define HPS_BODY(NN, EE)                                                                                        \
-        k_average_mothers_tiles_f64<NN, EE><<<grid, kMThreads, 0, s>>>(ch, mothers, fn, first_evt, n, ntiles, partials);
+        if (ntiles) {                                                                                           \
+            k_shift_mothers_f32<NN, EE><<<1, 32, 0, s>>>(ch, chf, fn, first_evt, mothers, k0);                  \
+            k_average_mothers_tiles_f32fix<NN, EE><<<grid, kTileThreads, 0, s>>>(ch, chf, fn, first_evt, n, ntiles, \
+                                                                                 partials, k0, mothers);        \
+        }                                                                                                       \
+        k_average_mothers_final_f32fix<NN, EE><<<1, kFinalThreads, 0, s>>>(ch, chf, fn, first_evt, partials, ntiles, out);
         HPS_DISPATCH_N_ENGINE(channel->n_daughters, channel->engine, HPS_BODY)
 #undef HPS_BODY
+    } else {
+        if (ntiles) {
+#define HPS_BODY(NN, EE)                                                                                        \
+            k_average_mothers_tiles_f64<NN, EE><<<grid, kMThreads, 0, s>>>(ch, mothers, fn, first_evt, n, ntiles, partials);
+            HPS_DISPATCH_N_ENGINE(channel->n_daughters, channel->engine, HPS_BODY)
+#undef HPS_BODY
+        }
+        k_average_mothers_final<<<1, 1024, 0, s>>>(partials, ntiles, out);
     }
-    k_average_mothers_final<<<1, 1024, 0, s>>>(partials, ntiles, out);
     st = cuda_status(cudaGetLastError(), "hps_average_on_mothers launch");
     if (owned) {
         cudaError_t e = cudaFreeAsync(scratch, s);

@@ -133,12 +133,37 @@ __device__ __forceinline__ float call_shift(const DevChannel& chd, const DevChan
 // fixed CTA tree adds the per-thread sums.  Result valid in thread 0.  With STORE, every event is
 // also stored (Generate and AverageOn of the same events in one pass): the sums are those of the
 // plain tile, bit for bit, and the stored events those of store_chunk_f32.
-template <int N, int ENGINE, bool STORE = false>
+// With MOTHERS (AverageMothers), event e is boosted by mothers[e] (a Vector4R column) and the
+// functor sees (mother, daughter 0, ..., daughter N-1).
+template <int N>
+__device__ __forceinline__ void load_mother(const double* __restrict__ mothers, uint64_t e, double (&mo)[4])
+{
+    const double2 a = __ldg(reinterpret_cast<const double2*>(mothers + 4 * e));
+    const double2 b = __ldg(reinterpret_cast<const double2*>(mothers + 4 * e) + 1);
+    mo[0] = a.x; mo[1] = a.y; mo[2] = b.x; mo[3] = b.y;
+}
+
+template <int N>
+__device__ __forceinline__ float mother_functor_f32(const DevFunctor& fn, const f32::MotherFrame& f,
+                                                    const float (&p)[N][4])
+{
+    float pm[N + 1][4];
+    pm[0][0] = f.e; pm[0][1] = f.px; pm[0][2] = f.py; pm[0][3] = f.pz;
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) pm[k + 1][c] = p[k][c];
+    return f32::functor<N + 1>(fn, pm);
+}
+
+template <int N, int ENGINE, bool STORE = false, bool MOTHERS = false>
 __device__ __forceinline__ hps_sums average_tile_f32(const DevChannel& chd, const DevChannelF& ch,
                                                      const DevFunctor& fn, uint64_t first, uint64_t n,
                                                      uint64_t t, float K0, void* smem,
-                                                     const StoreOut* so = nullptr)
+                                                     const StoreOut* so = nullptr,
+                                                     const double* __restrict__ mothers = nullptr)
 {
+    static_assert(!(STORE && MOTHERS), "a storing tile keeps the events in the decay's rest frame");
     float swh = 0.0f, swl = 0.0f, s1h = 0.0f, s1l = 0.0f, s2h = 0.0f, s2l = 0.0f;
     const uint64_t base = t * HPS_AVG_TILE;
     for (int k = 0; k < kAvgPerThread; ++k) {
@@ -152,7 +177,16 @@ __device__ __forceinline__ hps_sums average_tile_f32(const DevChannel& chd, cons
             const f32::EventWeight ew = f32::event_from_words<N, ENGINE>(chd, ch, w, p);
             if constexpr (STORE)
                 store_event_f32<N>(p, ew, so->cols, so->weights, so->flags, so->ukey, first, e, so->vec32 != 0);
-            const float d = f32::functor<N>(fn, p) - K0;
+            float d;
+            if constexpr (MOTHERS) {
+                double mo[4];
+                load_mother<N>(mothers, e, mo);
+                const f32::MotherFrame mf = f32::mother_frame(mo);
+                f32::boost_to_mother<N>(p, ch.m2, mf);
+                d = mother_functor_f32<N>(fn, mf, p) - K0;
+            } else {
+                d = f32::functor<N>(fn, p) - K0;
+            }
             // P*d and P*d^2 as float-float products
             const float h1 = ew.prod_hi * d;
             const float l1 = fmaf(ew.prod_lo, d, fmaf(ew.prod_hi, d, -h1));

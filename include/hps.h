@@ -208,7 +208,7 @@ hps_status hps_average_on_noalloc(const hps_channel* ch, uint64_t first_evt, uin
                                   const hps_functor* functor, hps_stats* out, int32_t precision,
                                   void* stream);
 
-/* Per-event mothers (FP64): mothers[n][4] is a device column of Vector4R, e.g. a daughter column
+/* Per-event mothers: mothers[n][4] is a device column of Vector4R, e.g. a daughter column
  * of an earlier hps_generate for a decay chain (examples/phase_space/phsp_chain.inl:216-238).
  *  hps_generate_mothers    Generate(mothers, daughters): DecayMothers (hydra/detail/functors/
  *                          DecayMothers.h:131-260), the stream and ECM of hps_generate, each event
@@ -217,7 +217,10 @@ hps_status hps_average_on_noalloc(const hps_channel* ch, uint64_t first_evt, uin
  *  hps_evaluate_mothers    Evaluate(mothers, result, functors): EvalMothers (EvalMothers.h:143-305):
  *                          engine seeded with hash(evt, seed) without discard, ECM and maximum
  *                          weight from each mother's mass.
- * The functor sees (mother, daughter 0, ..., daughter N-1): its indices count the mother as 0. */
+ * The functor sees (mother, daughter 0, ..., daughter N-1): its indices count the mother as 0.
+ * Precision: HPS_PREC_FP64 for all three; HPS_PREC_FP32_FIX for hps_generate_mothers and
+ * hps_average_on_mothers (the boost into each mother's frame in light-cone form, the mother's mass
+ * formed in float-float); hps_evaluate_mothers returns HPS_ERR_UNSUPPORTED for it. */
 hps_status hps_generate_mothers(const hps_channel* ch, uint64_t first_evt, uint64_t n, const double* mothers,
                                 double* const* cols, double* weights, int32_t precision, void* stream);
 hps_status hps_average_on_mothers(const hps_channel* ch, uint64_t first_evt, uint64_t n, const double* mothers,

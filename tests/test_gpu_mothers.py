@@ -77,9 +77,76 @@ def test_decay_chain_from_daughter_column(api, torch, oracle):
     assert np.abs(got.sum(axis=0) - mothers).max() <= 1e-12 * np.abs(mothers[:, 0]).max()
 
 
-def test_mothers_reject_fp32fix(api, torch, hps):
+def test_evalmothers_rejects_fp32fix(api, torch, hps):
     ch = api.make_channel([0.1, 0.2], 1.0, 1)
     mo = torch.zeros((4, 4), dtype=torch.float64, device="cuda")
-    four = torch.zeros((2, 4, 4), dtype=torch.float64, device="cuda")
+    w = torch.zeros(4, dtype=torch.float64, device="cuda")
     with pytest.raises(hps.HpsError, match="FP64 only"):
-        api.generate_mothers(ch, 0, mo, four, precision="fp32_fix")
+        api.evaluate_mothers(ch, 0, mo, [api.functor_one()], w, [torch.zeros_like(w)], precision="fp32_fix")
+
+
+FP32_TOL = 1e-6
+
+
+@pytest.mark.parametrize("name", MOTHER_GOLDEN)
+def test_mothers_fp32fix_within_tolerance(api, torch, oracle, name):
+    """DecayMothers and AverageMothers in FP32_FIX against the reference fixtures (the mothers move
+    with gamma up to about 1.03) within the precision contract of this form."""
+    g = load_golden(name)
+    N, n = int(g["N"]), int(g["n"])
+    ch = api.make_channel(list(g["masses"]), float(g["M"]), int(g["seed"]), int(g["engine"]))
+    mo = torch.as_tensor(g["mothers"], device="cuda")
+    four = torch.zeros((N, n, 4), dtype=torch.float64, device="cuda")
+    w = torch.zeros(n, dtype=torch.float64, device="cuda")
+    api.generate_mothers(ch, 0, mo, four, w, precision="fp32_fix")
+    torch.cuda.synchronize()
+    och = oracle.make_channel(g["masses"], float(g["M"]), int(g["seed"]), int(g["engine"]))
+    _, rw = oracle.generate_mothers(och, 0, g["mothers"])
+    e4 = enorm(four.cpu().numpy(), g["four"])
+    ew = float((np.abs(w.cpu().numpy() - rw) / rw).max())
+    print(f"\n[fp32_fix mothers] {name}: four {e4:.3e}, weight {ew:.3e}")
+    assert e4 <= FP32_TOL and ew <= FP32_TOL
+
+
+@pytest.mark.parametrize("gamma_p", [0.0, 1.0, 5.0, 40.0])
+def test_mothers_fp32fix_fast_mothers(api, torch, oracle, gamma_p):
+    """Mothers of mass 3.0969 with momentum up to 40 GeV (gamma about 13): the float-float mother
+    mass and the light-cone boost keep the error within the contract."""
+    n = 1 << 16
+    m = [0.1056583745, 0.1056583745, 0.13957]
+    M = 3.0969
+    rng = np.random.default_rng(7)
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    p = d * gamma_p * rng.uniform(0.5, 1.0, size=(n, 1))
+    mothers = np.concatenate([np.sqrt(M * M + (p * p).sum(axis=1, keepdims=True)), p], axis=1)
+    ch = api.make_channel(m, M, 0x3039, "philox")
+    och = oracle.make_channel(m, M, 0x3039, oracle.ENGINE_PHILOX)
+    four = torch.zeros((3, n, 4), dtype=torch.float64, device="cuda")
+    api.generate_mothers(ch, 0, torch.as_tensor(mothers, device="cuda"), four, None, precision="fp32_fix")
+    torch.cuda.synchronize()
+    rfour, _ = oracle.generate_mothers(och, 0, mothers)
+    e4 = enorm(four.cpu().numpy(), rfour)
+    print(f"\n[fp32_fix mothers] |p| up to {gamma_p}: four {e4:.3e}")
+    assert e4 <= FP32_TOL
+
+
+@pytest.mark.parametrize("engine", ["philox", "squares3"])
+def test_average_mothers_fp32fix(api, torch, oracle, engine):
+    n = 1 << 20
+    m = [0.493677, 0.13957, 0.13957]
+    M = 1.86484
+    rng = np.random.default_rng(11)
+    p = rng.normal(scale=0.8, size=(n, 3))
+    mothers = np.concatenate([np.sqrt(M * M + (p * p).sum(axis=1, keepdims=True)), p], axis=1)
+    ch = api.make_channel(m, M, 0x3039, engine)
+    och = oracle.make_channel(m, M, 0x3039, oracle.ENGINE_PHILOX if engine == "philox" else oracle.ENGINE_SQUARES3)
+    fn = api.functor_bw2(1, 2, 0.8955, 0.0473)     # K pi pair, indices count the mother as 0
+    out = torch.zeros(3, dtype=torch.float64, device="cuda")
+    api.average_on_mothers(ch, 0, torch.as_tensor(mothers, device="cuda"), fn, out, precision="fp32_fix")
+    mean, m2, W = out.cpu().tolist()
+    rmean, rm2, rW = oracle.average_mothers(och, oracle.make_functor(2, 1, 2, 0.8955, 0.0473), 0, mothers)
+    sigma = np.sqrt(rm2) / rW
+    print(f"\n[fp32_fix AverageMothers] {engine}: rel err mean {abs(mean - rmean) / abs(rmean):.3e}")
+    assert abs(mean - rmean) <= FP32_TOL * abs(rmean)
+    assert abs(mean - rmean) <= 3 * sigma
