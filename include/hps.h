@@ -220,7 +220,9 @@ hps_status hps_average_on_noalloc(const hps_channel* ch, uint64_t first_evt, uin
  * The functor sees (mother, daughter 0, ..., daughter N-1): its indices count the mother as 0.
  * Precision: HPS_PREC_FP64 for all three; HPS_PREC_FP32_FIX for hps_generate_mothers and
  * hps_average_on_mothers (the boost into each mother's frame in light-cone form, the mother's mass
- * formed in float-float); hps_evaluate_mothers returns HPS_ERR_UNSUPPORTED for it. */
+ * formed in float-float; the float errors of the rest-frame kinematics, about 5e-7 of the
+ * daughters' energies there, grow to about gamma * 5e-7 of a daughter thrown backwards by a mother
+ * of Lorentz factor gamma); hps_evaluate_mothers returns HPS_ERR_UNSUPPORTED for it. */
 hps_status hps_generate_mothers(const hps_channel* ch, uint64_t first_evt, uint64_t n, const double* mothers,
                                 double* const* cols, double* weights, int32_t precision, void* stream);
 hps_status hps_average_on_mothers(const hps_channel* ch, uint64_t first_evt, uint64_t n, const double* mothers,
