@@ -172,9 +172,12 @@ def barrier(world):
 
 def cpu_sample(seconds=3.0, n_sample=1 << 21, nthreads=0):
     """Oracle port of the reference (FP64, -O3, OpenMP over all host threads): store step +
-    AverageOn on chunks of the workload until `seconds` of wall time have elapsed."""
+    AverageOn on chunks of the workload until `seconds` of wall time have elapsed.  All host
+    cores are used even when a launcher (torchrun) has set OMP_NUM_THREADS=1 for its ranks."""
     import numpy as np
     from oracle import oracle as O
+    if nthreads <= 0:
+        nthreads = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
     O.build()
     ch = O.make_channel(MASSES, MOTHER, SEED, O.ENGINE_PHILOX)
     fn = O.make_functor(2, *BW)
