@@ -182,6 +182,24 @@ template <> struct is_menu<BW2> : std::true_type {};
 
 // --------------------------------------------------------------------------------- Decays
 
+// Column selectors of the reference (hydra/Placeholders.h): hydra::placeholders::_0 ... _9.
+namespace placeholders {
+template <unsigned I> struct placeholder { static constexpr unsigned index = I; };
+static const placeholder<0> _0{}; static const placeholder<1> _1{}; static const placeholder<2> _2{};
+static const placeholder<3> _3{}; static const placeholder<4> _4{}; static const placeholder<5> _5{};
+static const placeholder<6> _6{}; static const placeholder<7> _7{}; static const placeholder<8> _8{};
+static const placeholder<9> _9{};
+}  // namespace placeholders
+
+// One daughter column of a Decays, as Decays::GetDaugtherRange(_k) hands it out (a range of
+// Vector4R): here its raw pointer ({E,px,py,pz} per event), its length and where it lives.
+struct DaughterRange {
+    const double* data;
+    size_t n;
+    bool on_device;
+    size_t size() const { return n; }
+};
+
 template <typename Tuple, typename Backend> class Decays;
 
 template <typename... Particles, typename Backend>
@@ -230,6 +248,15 @@ public:
             p[k].set(v[0], v[1], v[2], v[3]);
         }
         return make(p, std::index_sequence_for<Particles...>{});
+    }
+
+    // Decays::GetDaugtherRange(placeholder) (hydra/Decays.h:279-284): daughter I's column, e.g.
+    // the mothers of the next step of a decay chain (examples/phase_space/phsp_chain.inl:236).
+    template <unsigned I>
+    DaughterRange GetDaugtherRange(placeholders::placeholder<I>) const
+    {
+        static_assert(I < nparticles, "no such daughter");
+        return DaughterRange{column(I), fN, on_device};
     }
 
     // Raw column k ({E,px,py,pz} per event) and the weight column.
@@ -566,6 +593,88 @@ public:
                 detail::throw_cuda(cudaMemcpy(result.column(k), out[k], n * 8, cudaMemcpyDeviceToHost), "cudaMemcpy");
     }
 
+    // Generate(mothers, daughters) (PhaseSpace.inl:399-417, DecayMothers): event i is boosted by
+    // mothers[i]; the stream, ECM and weights are those of Generate(mother, daughters).
+    template <typename... P, typename Backend>
+    void Generate(DaughterRange const& mothers, Decays<hydra::tuple<P...>, Backend>& events)
+    {
+        static_assert(sizeof...(P) == N, "Decays must hold N daughters");
+        if (mothers.n != events.size()) throw std::invalid_argument("[hydra::PhaseSpace]: mothers and daughters differ in size");
+        hps_channel ch = channel(Vector4R(fMotherMass, 0, 0, 0));
+        detail::DeviceBuffer<double> tmo;
+        const double* mo = device_mothers(mothers, tmo);
+        const bool dev = Decays<hydra::tuple<P...>, Backend>::on_device;
+        std::vector<detail::DeviceBuffer<double>> tmp;
+        double* cols[N];
+        for (size_t k = 0; k < N; ++k) {
+            if (dev) {
+                cols[k] = events.column(k);
+            } else {
+                tmp.emplace_back(4 * events.size());
+                cols[k] = tmp.back().p;
+            }
+        }
+        detail::DeviceBuffer<double> tw(dev ? 0 : events.size());
+        detail::throw_status(hps_generate_mothers(&ch, 0, events.size(), mo, cols, dev ? events.weights() : tw.p,
+                                                  fPrecision, nullptr));
+        detail::throw_cuda(cudaStreamSynchronize(nullptr), "cudaStreamSynchronize");
+        if (!dev) {
+            for (size_t k = 0; k < N; ++k)
+                detail::throw_cuda(cudaMemcpy(events.column(k), cols[k], events.size() * 32, cudaMemcpyDeviceToHost),
+                                   "cudaMemcpy");
+            detail::throw_cuda(cudaMemcpy(events.weights(), tw.p, events.size() * 8, cudaMemcpyDeviceToHost),
+                               "cudaMemcpy");
+        }
+    }
+
+    // AverageOn(mothers, functor) (PhaseSpace.inl:276-287, AverageMothers): the functor sees
+    // (mother, daughter 0, ..., daughter N-1).
+    template <typename Functor>
+    std::pair<GReal_t, GReal_t> AverageOn(DaughterRange const& mothers, Functor const& functor)
+    {
+        static_assert(hps_fn::is_menu<Functor>::value,
+                      "AverageOn across the C ABI takes hydra::hps_fn::One, Mass2 or BW2");
+        hps_channel ch = channel(Vector4R(fMotherMass, 0, 0, 0));
+        detail::DeviceBuffer<double> tmo;
+        const double* mo = device_mothers(mothers, tmo);
+        detail::DeviceBuffer<hps_stats> out(1);
+        detail::throw_status(hps_average_on_mothers(&ch, 0, mothers.n, mo, &functor.f, out.p, nullptr, 0, fPrecision,
+                                                    nullptr));
+        hps_stats st;
+        detail::throw_cuda(cudaMemcpy(&st, out.p, sizeof(st), cudaMemcpyDeviceToHost), "cudaMemcpy");
+        return std::make_pair(st.mean, std::sqrt(st.m2) / st.w);
+    }
+
+    // Evaluate(mothers, result, functors...) (PhaseSpace.inl:334-348, EvalMothers): its own stream
+    // per event (hash(event, seed)), ECM and maximum weight from each mother's mass; FP64 only.
+    template <typename... T, typename Backend, typename... Functors>
+    void Evaluate(DaughterRange const& mothers, multivector<hydra::tuple<T...>, Backend>& result, Functors const&... fs)
+    {
+        static_assert(sizeof...(T) == sizeof...(Functors) + 1, "one result column per functor plus the weight");
+        const hps_functor menu[] = {fs.f...};
+        hps_channel ch = channel(Vector4R(fMotherMass, 0, 0, 0));
+        detail::DeviceBuffer<double> tmo;
+        const double* mo = device_mothers(mothers, tmo);
+        const size_t n = mothers.n;
+        const bool dev = multivector<hydra::tuple<T...>, Backend>::on_device;
+        std::vector<detail::DeviceBuffer<double>> tmp;
+        double* out[sizeof...(Functors) + 1];
+        for (size_t k = 0; k <= sizeof...(Functors); ++k) {
+            if (dev) {
+                out[k] = result.column(k);
+            } else {
+                tmp.emplace_back(n);
+                out[k] = tmp.back().p;
+            }
+        }
+        detail::throw_status(hps_evaluate_mothers(&ch, 0, n, mo, menu, sizeof...(Functors), out[0], out + 1,
+                                                  HPS_PREC_FP64, nullptr));
+        detail::throw_cuda(cudaStreamSynchronize(nullptr), "cudaStreamSynchronize");
+        if (!dev)
+            for (size_t k = 0; k <= sizeof...(Functors); ++k)
+                detail::throw_cuda(cudaMemcpy(result.column(k), out[k], n * 8, cudaMemcpyDeviceToHost), "cudaMemcpy");
+    }
+
     GInt_t GetSeed() const { return static_cast<GInt_t>(fSeed); }
     void SetSeed(GInt_t seed) { fSeed = static_cast<size_t>(static_cast<long long>(seed)); }
     const GReal_t* GetMasses() const { return fMasses; }
@@ -597,6 +706,16 @@ private:
         fMaxWeight = ch.max_weight;
         // default seed: 1 * (1 + hash_range(masses)) (PhaseSpace.inl:44,64)
         fSeed = hps_default_seed(N, masses);
+    }
+
+    // The mothers column on the device (copied there for a host Decays).
+    static const double* device_mothers(DaughterRange const& m, detail::DeviceBuffer<double>& tmp)
+    {
+        if (m.on_device) return m.data;
+        tmp.resize(4 * m.n);
+        if (m.n)
+            detail::throw_cuda(cudaMemcpy(tmp.p, m.data, m.n * 32, cudaMemcpyHostToDevice), "cudaMemcpy");
+        return tmp.p;
     }
 
     hps_channel channel(Vector4R const& mother) const

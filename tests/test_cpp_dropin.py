@@ -14,6 +14,7 @@ from conftest import REPO, load_golden
 
 SRC = REPO / "tests" / "cpp" / "phsp_dropin.cpp"
 SRC_EXTRAS = REPO / "tests" / "cpp" / "phsp_extras.cpp"
+SRC_CHAIN = REPO / "tests" / "cpp" / "phsp_chain.cpp"
 
 
 def cuda_home():
@@ -91,3 +92,33 @@ def test_extras_example_matches_reference(hps, cuda, tmp_path):
     assert np.array_equal(np.array(d["range_w"]), g["range_w"])
     rf = four("range_four")
     assert float((np.abs(rf - g["range_four"]).max(axis=2) / np.abs(g["range_four"][:, :, 0])).max()) <= 1e-12
+
+
+def test_chain_example_compiles(hps, tmp_path):
+    assert compile_example(hps, tmp_path / "phsp_chain", SRC_CHAIN).exists()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol", [(0, 1e-12), (1, 1e-6)])
+def test_chain_example_matches_oracle(hps, cuda, oracle, tmp_path, precision, tol):
+    """Generate(GetDaugtherRange(_0), events), AverageOn(mothers, f) and Evaluate(mothers, ...)
+    through the C++ headers against the oracle's DecayMothers / AverageMothers / EvalMothers on the
+    J/psi column the program produced."""
+    n = 2048
+    exe = compile_example(hps, tmp_path / "phsp_chain", SRC_CHAIN)
+    r = subprocess.run([str(exe), str(n), str(precision)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    d = json.loads(r.stdout)
+    jpsi = np.array(d["jpsi"]).reshape(n, 4)
+    mu = np.stack([np.array(d["mup"]).reshape(n, 4), np.array(d["mum"]).reshape(n, 4)])
+    och = oracle.make_channel([0.1056583745, 0.1056583745], 3.0969, 0x3040, oracle.ENGINE_PHILOX)
+    rfour, _ = oracle.generate_mothers(och, 0, jpsi)
+    err = float((np.abs(mu - rfour).max(axis=2) / np.abs(rfour[:, :, 0])).max())
+    assert err <= tol, err
+    # the muons add up to their J/psi
+    assert np.abs(mu.sum(axis=0) - jpsi).max() <= 10 * tol * np.abs(jpsi[:, 0]).max()
+    rmean, rm2, rW = oracle.average_mothers(och, oracle.make_functor(1, 1, 2), 0, jpsi)
+    assert abs(d["avg_mean"] - rmean) <= max(tol, 1e-10) * abs(rmean)
+    rw, rf, _ = oracle.evaluate_mothers(och, oracle.make_functor(1, 0, 1), 0, jpsi)
+    assert np.array_equal(np.array(d["eval_w"]), rw)
+    np.testing.assert_allclose(d["eval_f"], rf, rtol=1e-12, atol=0)
