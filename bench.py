@@ -303,8 +303,9 @@ def run_gpu(args):
         hstats = torch.zeros(3, dtype=torch.float64).pin_memory()
 
         def e2e_step():
-            api.generate_host(ch, first, hfour, hw, hfl, UNWEIGHT_SEED, args.precision, 0, stream)
-            api.average_on(ch, first, n, fn, stats, ws, args.precision, stream)
+            # Generate into pinned host Decays and AverageOn of the same events: one kernel writes
+            # the events across the link and reduces meanwhile (hps_generate_average_host)
+            api.generate_average_host(ch, first, hfour, hw, hfl, fn, stats, UNWEIGHT_SEED, args.precision, stream)
             hstats.copy_(stats, non_blocking=True)
             stream.synchronize()
 
@@ -319,7 +320,7 @@ def run_gpu(args):
         dt = max_over_ranks(time.perf_counter() - t0, world)
         e2e = {"value": world * n * e2e_steps / dt, "unit": "events/s", "h2d_bytes_per_step": 0,
                "d2h_bytes_per_step": n * BYTES_PER_EVENT + 24, "steps": e2e_steps,
-               "note": "hps_generate_host into pinned host Decays + AverageOn result read back"}
+               "note": "hps_generate_average_host: Decays into pinned host memory + AverageOn, result read back"}
 
     peak, peak_kind = measured_peak_hbm()
     gen_avg_s = statistics.mean(gen_ms) / 1e3

@@ -165,6 +165,8 @@ SIGNATURES = {
     "hps_compact_workspace_size": (_sz, [_u64]),
     "hps_unweight_compact": (_i32, [_i32, _u64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "hps_rng_words": (_i32, [_i32, _i32, _u64, _u64, _u64, _vp, _vp]),
+    "hps_generate_average_host": (_i32, [ctypes.POINTER(HpsChannel), _u64, _u64, _vp, _vp, _vp, _u64,
+                                         ctypes.POINTER(HpsFunctor), _vp, _i32, _vp]),
     "hps_generate_average": (_i32, [ctypes.POINTER(HpsChannel), _u64, _u64, _vp, _vp, _vp, _u64,
                                     ctypes.POINTER(HpsFunctor), _vp, _vp, _sz, _i32, _vp]),
     "hps_reweight": (_i32, [_i32, _vp, _dbl, ctypes.POINTER(HpsFunctor), _u64, _vp, _vp, _vp, _vp]),

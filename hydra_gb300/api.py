@@ -184,6 +184,22 @@ def generate_average(ch: HpsChannel, first: int, four: torch.Tensor, weights, fl
                                      _dptr(workspace), wbytes, _PRECISIONS[precision], _stream_handle(stream)))
 
 
+def generate_average_host(ch: HpsChannel, first: int, four: torch.Tensor, weights, flags, functor: HpsFunctor,
+                          out: torch.Tensor, unweight_seed: int = DEFAULT_UNWEIGHT_SEED, precision="fp64",
+                          stream=None) -> None:
+    """generate_host and average_on of the same events; with pinned host tensors in one pass.
+    four/weights/flags: CPU tensors; out: 3-element float64 CUDA tensor.  Synchronous."""
+    if four.is_cuda or four.dtype != torch.float64 or four.dim() != 3 or not four.is_contiguous():
+        raise ValueError("four must be a contiguous CPU float64 [N, n, 4] tensor")
+    N, n = four.shape[0], four.shape[1]
+    arr = (ctypes.c_void_p * N)(*[four[k].data_ptr() for k in range(N)])
+    wp = ctypes.c_void_p(weights.data_ptr()) if weights is not None else ctypes.c_void_p(0)
+    fp = ctypes.c_void_p(flags.data_ptr()) if flags is not None else ctypes.c_void_p(0)
+    check(lib().hps_generate_average_host(ctypes.byref(ch), first, n, ctypes.cast(arr, ctypes.c_void_p), wp, fp,
+                                          unweight_seed & (2**64 - 1), ctypes.byref(functor), _dptr(out),
+                                          _PRECISIONS[precision], _stream_handle(stream)))
+
+
 def generate_mothers(ch: HpsChannel, first: int, mothers: torch.Tensor, four: torch.Tensor, weights=None,
                      precision="fp64", stream=None) -> None:
     """DecayMothers: mothers [n, 4] (a Vector4R column), four [N, n, 4]."""

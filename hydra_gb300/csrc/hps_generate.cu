@@ -223,6 +223,29 @@ static hps_status copy_stream(cudaStream_t* out)
 
 }  // namespace hps
 
+namespace hps {
+
+// Device addresses of pinned, device-mapped host buffers; false if any buffer is not one.
+static bool map_host_outputs(int N, double* const* host_cols, double* host_weights, uint8_t* host_flags,
+                             double** dcols, double** dw, uint8_t** df)
+{
+    bool mapped = true;
+    auto map = [&](void* h, void** d) {
+        *d = nullptr;
+        if (!h || !mapped) return;
+        if (cudaHostGetDevicePointer(d, h, 0) != cudaSuccess) {
+            cudaGetLastError();
+            mapped = false;
+        }
+    };
+    for (int k = 0; k < N; ++k) map(host_cols[k], reinterpret_cast<void**>(&dcols[k]));
+    map(host_weights, reinterpret_cast<void**>(dw));
+    map(host_flags, reinterpret_cast<void**>(df));
+    return mapped;
+}
+
+}  // namespace hps
+
 extern "C" hps_status hps_generate_host(const hps_channel* channel, uint64_t first_evt, uint64_t n,
                                         double* const* host_cols, double* host_weights, uint8_t* host_flags,
                                         uint64_t unweight_seed, int32_t precision, uint64_t chunk_events,
@@ -242,22 +265,10 @@ extern "C" hps_status hps_generate_host(const hps_channel* channel, uint64_t fir
         // Direct mode: when every host buffer is pinned, device-mapped memory, the kernel writes
         // the Decays straight into it across the CPU-GPU link -- no staging copy, no copy engine.
         double* dcols[HPS_MAX_DAUGHTERS];
-        bool mapped = true;
-        auto map = [&](void* h, void** d) {
-            if (!h) { *d = nullptr; return; }
-            if (cudaHostGetDevicePointer(d, h, 0) != cudaSuccess) {
-                cudaGetLastError();
-                mapped = false;
-            }
-        };
-        for (int k = 0; k < N && mapped; ++k) map(host_cols[k], reinterpret_cast<void**>(&dcols[k]));
-        void* dw = nullptr;
-        void* df = nullptr;
-        if (mapped) map(host_weights, &dw);
-        if (mapped) map(host_flags, &df);
-        if (mapped) {
-            st = hps_generate(channel, first_evt, n, dcols, static_cast<double*>(dw), static_cast<uint8_t*>(df),
-                              unweight_seed, precision, stream);
+        double* dw = nullptr;
+        uint8_t* df = nullptr;
+        if (map_host_outputs(N, host_cols, host_weights, host_flags, dcols, &dw, &df)) {
+            st = hps_generate(channel, first_evt, n, dcols, dw, df, unweight_seed, precision, stream);
             if (st != HPS_OK) return st;
             return cuda_status(cudaStreamSynchronize(as_stream(stream)), "cudaStreamSynchronize");
         }
@@ -319,4 +330,34 @@ extern "C" hps_status hps_generate_host(const hps_channel* channel, uint64_t fir
     e = cudaStreamSynchronize(s);
     if (st == HPS_OK && e != cudaSuccess) st = cuda_status(e, "cudaStreamSynchronize");
     return st;
+}
+
+extern "C" hps_status hps_generate_average_host(const hps_channel* channel, uint64_t first_evt, uint64_t n,
+                                                double* const* host_cols, double* host_weights, uint8_t* host_flags,
+                                                uint64_t unweight_seed, const hps_functor* functor, hps_stats* out,
+                                                int32_t precision, void* stream)
+{
+    clear_error();
+    DevChannel ch;
+    hps_status st = to_device_channel(channel, &ch);
+    if (st != HPS_OK) return st;
+    if (!host_cols && n) return set_error(HPS_ERR_BAD_ARG, "host_cols is NULL");
+    const int N = channel->n_daughters;
+    for (int k = 0; k < N && n; ++k)
+        if (!host_cols[k]) return set_error(HPS_ERR_BAD_ARG, "host column %d is NULL", k);
+    double* dcols[HPS_MAX_DAUGHTERS] = {};
+    double* dw = nullptr;
+    uint8_t* df = nullptr;
+    if (n && map_host_outputs(N, host_cols, host_weights, host_flags, dcols, &dw, &df)) {
+        // one pass: the kernel writes the Decays across the link and reduces AverageOn meanwhile
+        st = hps_generate_average(channel, first_evt, n, dcols, dw, df, unweight_seed, functor, out, nullptr, 0,
+                                  precision, stream);
+    } else {
+        st = hps_generate_host(channel, first_evt, n, host_cols, host_weights, host_flags, unweight_seed, precision, 0,
+                               stream);
+        if (st == HPS_OK)
+            st = hps_average_on(channel, first_evt, n, functor, out, nullptr, 0, precision, stream);
+    }
+    if (st != HPS_OK) return st;
+    return cuda_status(cudaStreamSynchronize(as_stream(stream)), "cudaStreamSynchronize");
 }

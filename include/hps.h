@@ -188,6 +188,15 @@ hps_status hps_generate_average(const hps_channel* ch, uint64_t first_evt, uint6
                                 const hps_functor* functor, hps_stats* out, void* workspace,
                                 size_t workspace_bytes, int32_t precision, void* stream);
 
+/* hps_generate_average with the Decays, weights and flags in HOST memory (like hps_generate_host):
+ * with pinned, device-mapped host buffers one kernel writes the events across the CPU-GPU link and
+ * reduces AverageOn meanwhile; otherwise hps_generate_host then hps_average_on.  out is a device
+ * pointer; the call returns when both results are complete. */
+hps_status hps_generate_average_host(const hps_channel* ch, uint64_t first_evt, uint64_t n,
+                                     double* const* host_cols, double* host_weights, uint8_t* host_flags,
+                                     uint64_t unweight_seed, const hps_functor* functor, hps_stats* out,
+                                     int32_t precision, void* stream);
+
 /* AverageOn that makes no device allocation at all (no counterpart in the reference; Hydra's
  * own reduction always takes temporary storage from its allocator).  It is meant for host
  * programs that may not allocate device memory once they are running -- for example a

@@ -61,3 +61,26 @@ def test_fused_without_weights_and_flags(api, torch):
     api.average_on(ch, 0, n, fn, s1, None, "fp32_fix")
     torch.cuda.synchronize()
     assert torch.equal(f, f1) and s.tolist() == s1.tolist()
+
+
+@pytest.mark.parametrize("pinned", [True, False])
+def test_fused_host_equals_separate_calls(api, torch, pinned):
+    ch = api.make_channel([K, PI, PI, PI, PI], 1.86484, 0x3039, "philox")
+    fn = api.functor_bw2(0, 1, 0.8955, 0.0473)
+    n = 300_001
+    f1 = torch.empty((5, n, 4), dtype=torch.float64, device="cuda")
+    w1 = torch.empty(n, dtype=torch.float64, device="cuda")
+    g1 = torch.empty(n, dtype=torch.uint8, device="cuda")
+    s1 = torch.zeros(3, dtype=torch.float64, device="cuda")
+    api.generate(ch, 5, f1, w1, g1, precision="fp32_fix")
+    api.average_on(ch, 5, n, fn, s1, None, "fp32_fix")
+    hf = torch.zeros((5, n, 4), dtype=torch.float64)
+    hw = torch.zeros(n, dtype=torch.float64)
+    hg = torch.zeros(n, dtype=torch.uint8)
+    if pinned:
+        hf, hw, hg = hf.pin_memory(), hw.pin_memory(), hg.pin_memory()
+    s2 = torch.zeros(3, dtype=torch.float64, device="cuda")
+    api.generate_average_host(ch, 5, hf, hw, hg, fn, s2, precision="fp32_fix")
+    torch.cuda.synchronize()
+    assert torch.equal(f1.cpu(), hf) and torch.equal(w1.cpu(), hw) and torch.equal(g1.cpu(), hg)
+    assert s1.tolist() == s2.tolist()
