@@ -168,3 +168,32 @@ def test_consumer_arguments_rejected_before_launch(hps):
     assert st == hps.ERR_BAD_ARG and b"kind" in lib.hps_last_error()
     st = lib.hps_weight_flags(10, None, 1.0, None, 0, 0, None, None)
     assert st == hps.ERR_BAD_ARG
+
+
+def test_fused_and_mothers_arguments_rejected_before_launch(hps):
+    """hps_generate_average(_host) and the FP32_FIX mother forms validate on the host."""
+    from hydra_gb300 import api
+    lib = hps.lib()
+    ch = api.make_channel([0.1, 0.2, 0.3], 1.0, 1)
+    fn = api.functor_mass2(0, 1)
+    out = ctypes.c_void_p(1024)
+    cols = (ctypes.c_void_p * 3)(256, 512 + 8, 768)            # column 1 misaligned, never dereferenced
+    st = lib.hps_generate_average(ctypes.byref(ch), 0, 10, ctypes.cast(cols, ctypes.c_void_p), None, None, 0,
+                                  ctypes.byref(fn), out, None, 0, 1, None)
+    assert st == hps.ERR_BAD_ARG and b"aligned" in lib.hps_last_error()
+    bad = api.functor_mass2(0, 5)
+    st = lib.hps_generate_average(ctypes.byref(ch), 0, 10, None, None, None, 0, ctypes.byref(bad), out, None, 0, 1,
+                                  None)
+    assert st == hps.ERR_BAD_ARG and b"indices" in lib.hps_last_error()
+    st = lib.hps_generate_average(ctypes.byref(ch), 0, 10, None, None, None, 0, ctypes.byref(fn), out, None, 0, 9,
+                                  None)
+    assert st == hps.ERR_BAD_ARG and b"precision" in lib.hps_last_error()
+    st = lib.hps_generate_average_host(ctypes.byref(ch), 0, 10, None, None, None, 0, ctypes.byref(fn), out, 1, None)
+    assert st == hps.ERR_BAD_ARG and b"host_cols" in lib.hps_last_error()
+    # EvalMothers has no FP32_FIX form; DecayMothers / AverageMothers do
+    mo = ctypes.c_void_p(2048)
+    w = ctypes.c_void_p(4096)
+    st = lib.hps_evaluate_mothers(ctypes.byref(ch), 0, 10, mo, ctypes.byref(fn), 1, w, None, 1, None)
+    assert st == hps.ERR_UNSUPPORTED and b"FP64 only" in lib.hps_last_error()
+    st = lib.hps_generate_mothers(ctypes.byref(ch), 0, 10, mo, None, None, 7, None)
+    assert st == hps.ERR_BAD_ARG and b"precision" in lib.hps_last_error()
