@@ -57,6 +57,9 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
+DEFAULT_N = 1 << 24          # events per step of the bench workload (config 2)
+
+
 def profiled_traffic(precision):
     """DRAM bytes per launch of the store kernel from the committed ncu summary, if any."""
     p = REPO / "profiles" / "traffic.json"
@@ -325,7 +328,7 @@ def run_gpu(args):
     peak, peak_kind = measured_peak_hbm()
     gen_avg_s = statistics.mean(gen_ms) / 1e3
     achieved = n * BYTES_PER_EVENT / gen_avg_s / 1e9
-    traffic = profiled_traffic(args.precision)
+    traffic = profiled_traffic(args.precision) if n == DEFAULT_N else None   # captured for the default size
     roofline = {"bound": "hbm", "kernel": "k_generate (store path)", "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                 "traffic": traffic, "algorithmic_bytes_per_launch": n * BYTES_PER_EVENT,
@@ -402,7 +405,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--precision", choices=["fp64", "fp32_fix"], default="fp32_fix")
-    ap.add_argument("--n", type=int, default=1 << 24)
+    ap.add_argument("--n", type=int, default=DEFAULT_N)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-check", action="store_true")
