@@ -7,6 +7,9 @@
 #
 #   ref_harness_cpp : HYDRA_DEVICE_SYSTEM=CPP, sequential, -ffp-contract=off (parity build)
 #   ref_harness_omp : HYDRA_DEVICE_SYSTEM=OMP, all host threads, -ffp-contract=off
+#   ref_gpu.cubin   : the reference's DecayMother / AverageMother device code for sm_103a
+#                     (oracle/ref_gpu.cu, the reference build's nvcc flags); loaded by
+#                     oracle/ref_gpu.py on a GPU host, which needs no Hydra sources
 set -euo pipefail
 here="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 src="${HYDRA_SRC:-/root/reference}"
@@ -16,12 +19,19 @@ if [ ! -f "$src/hydra/PhaseSpace.h" ]; then
     exit 0
 fi
 mkdir -p "$out"
-if [ "$out/ref_harness_cpp" -nt "$here/ref_harness.cpp" ] && [ "$out/ref_harness_omp" -nt "$here/ref_harness.cpp" ]; then
-    echo "build_ref.sh: $out up to date"
-    exit 0
-fi
+nvcc="${NVCC:-$(command -v nvcc || echo /usr/local/cuda/bin/nvcc)}"
+pids=()
 common=(-std=c++17 -O2 -ffp-contract=off -fno-fast-math -w -I"$src" -DHYDRA_HOST_SYSTEM=CPP)
-g++ "${common[@]}" -DHYDRA_DEVICE_SYSTEM=CPP "$here/ref_harness.cpp" -o "$out/ref_harness_cpp" &
-g++ "${common[@]}" -fopenmp -DHYDRA_DEVICE_SYSTEM=OMP "$here/ref_harness.cpp" -o "$out/ref_harness_omp" &
-wait -n && wait -n
-echo "build_ref.sh: built $out/ref_harness_cpp $out/ref_harness_omp"
+if ! [ "$out/ref_harness_cpp" -nt "$here/ref_harness.cpp" ]; then
+    g++ "${common[@]}" -DHYDRA_DEVICE_SYSTEM=CPP "$here/ref_harness.cpp" -o "$out/ref_harness_cpp" & pids+=($!)
+fi
+if ! [ "$out/ref_harness_omp" -nt "$here/ref_harness.cpp" ]; then
+    g++ "${common[@]}" -fopenmp -DHYDRA_DEVICE_SYSTEM=OMP "$here/ref_harness.cpp" -o "$out/ref_harness_omp" & pids+=($!)
+fi
+if ! [ "$out/ref_gpu.cubin" -nt "$here/ref_gpu.cu" ]; then
+    "$nvcc" -std=c++20 -O3 --extended-lambda --expt-relaxed-constexpr -w -gencode arch=compute_103a,code=sm_103a \
+        -I"$src" -DHYDRA_HOST_SYSTEM=CPP -DHYDRA_DEVICE_SYSTEM=CUDA -cubin "$here/ref_gpu.cu" \
+        -o "$out/ref_gpu.cubin" & pids+=($!)
+fi
+for p in "${pids[@]}"; do wait "$p"; done
+echo "build_ref.sh: $out up to date (ref_harness_cpp, ref_harness_omp, ref_gpu.cubin)"
