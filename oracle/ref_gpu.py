@@ -17,6 +17,7 @@ to build; where it is absent ``available()`` is False.
 from __future__ import annotations
 
 import ctypes
+import functools
 from pathlib import Path
 
 import numpy as np
@@ -32,6 +33,7 @@ def available() -> bool:
     return CUBIN.exists()
 
 
+@functools.lru_cache(maxsize=None)
 def _mother_args(n: int):
     class MotherArgs(ctypes.Structure):
         _fields_ = [("seed", ctypes.c_uint64), ("ecm", ctypes.c_double), ("maxw", ctypes.c_double),
@@ -126,6 +128,13 @@ def add_stats(x, y):
     return ((x[0] * x[2] + y[0] * y[2]) / w, x[1] + y[1] + delta * delta * x[2] * y[2] / w, w)
 
 
+@functools.lru_cache(maxsize=None)
+def _avg_args(n: int):
+    class AvgArgs(ctypes.Structure):
+        _fields_ = [("m", _mother_args(n)), ("f", _BW)]
+    return AvgArgs
+
+
 def average_bw_partials(ch, i: int, j: int, a: float, b: float, first: int, n: int):
     """Launches the reference's AverageMother; returns the (blocks, 3) float64 cuda tensor
     of per-block StatsPHSP {mean, M2, W}."""
@@ -134,9 +143,7 @@ def average_bw_partials(ch, i: int, j: int, a: float, b: float, first: int, n: i
     grid = max(1, min((n + THREADS - 1) // THREADS, AVG_BLOCKS))
     partial = torch.empty((grid, 3), dtype=torch.float64, device="cuda")
 
-    class AvgArgs(ctypes.Structure):
-        _fields_ = [("m", _mother_args(N)), ("f", _BW)]
-    args = AvgArgs()
+    args = _avg_args(N)()
     args.m = _args(ch)
     args.f = _BW(i, j, a, b)
     _launch(f"ref_average_bw_{N}_{ENGINES[ch.engine]}", grid,
@@ -179,9 +186,10 @@ def _time(fn, steps: int, warmup: int) -> float:
 
 def main(argv=None):
     """Times the reference's CUDA functors at the benchmark workloads (one JSON line each):
-    N=5 D0 -> K pi pi pi pi (2^24 events, Generate and AverageOn |BW(m_K pi)|^2) and the
-    N=3 B0 -> J/psi K pi / N=10 pion cases (2^26 events, Generate).  Outputs of 2^26
-    events (21.5 GB at N=10) exceed the L2, so no flush is needed between steps."""
+    N=5 D0 -> K pi pi pi pi (2^24 events, Generate and AverageOn |BW(m_K pi)|^2), the
+    N=3 B0 -> J/psi K pi channel (10^6 and 2^26 events) and ten pions (2^26 events), Generate.
+    Every output but the 10^6-event one (96 MB) exceeds the L2; the time of that one includes
+    whatever of the previous step's output the L2 still holds."""
     import argparse
     import json
     import sys
@@ -198,6 +206,7 @@ def main(argv=None):
     cases = [
         ("generate", "N5_D0_Kpipipipi", [K, pi, pi, pi, pi], 1.86484, 1 << 24),
         ("average_bw", "N5_D0_Kpipipipi", [K, pi, pi, pi, pi], 1.86484, 1 << 24),
+        ("generate", "N3_B0_JpsiKpi", [3.0969, K, pi], 5.27934, 10 ** 6),
         ("generate", "N3_B0_JpsiKpi", [3.0969, K, pi], 5.27934, 1 << 26),
         ("generate", "N10_pions", [pi] * 10, 5.0, 1 << 26),
     ]

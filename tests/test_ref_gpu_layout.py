@@ -17,8 +17,9 @@ def test_mother_args_layout(n):
     assert ctypes.sizeof(M) == 8 * (6 + n)
     assert M.ecm.offset == 8 and M.maxw.offset == 16 and M.beta.offset == 24 and M.masses.offset == 48
 
-    class A(ctypes.Structure):
-        _fields_ = [("m", M), ("f", ref_gpu._BW)]
+    A = ref_gpu._avg_args(n)
+    a = A()
+    a.m = M()                     # the cached classes are the same type on every call
     assert A.f.offset == 8 * (6 + n)
     assert ctypes.sizeof(A) == 8 * (6 + n) + 24
     assert ref_gpu._BW.a.offset == 8
