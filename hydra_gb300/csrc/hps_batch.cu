@@ -1,13 +1,17 @@
 // hps_batch.cu -- many channels of different N in one persistent, graph-captured launch.
 //
 // The items of a plan are cut into work units: a store item into units of store_tile events,
-// an AverageOn item into tiles of HPS_AVG_TILE events.  A persistent grid of 256-thread CTAs
-// takes units from a device counter; each unit dispatches on (N, engine, mode) to the same
-// work-unit functions the single-channel FP32_FIX kernels use (tiles_f32.cuh), so an item's
-// outputs do not depend on what else is in the batch.  A second kernel merges each AverageOn
-// item's tile partials with the fixed tree of hps_average_on.  Counter reset, persistent kernel
-// and merge are captured once into a CUDA graph; the item table and its header live in device
-// memory, so new items need no re-capture.
+// an AverageOn item into tiles of HPS_AVG_TILE events.  Items are grouped by register class of N
+// (2-5, 6-7, 8-9, 10): one persistent kernel per class, so a class runs at the occupancy its own
+// register count allows (one kernel over every N would hold every channel to the registers of
+// N = 10).  The class kernels run as parallel branches of the graph, so the SMs one class frees
+// at its end take CTAs of the others.  A class kernel's 256-thread CTAs take units from the
+// class's device counter; each unit dispatches on (N, engine, mode) to the same work-unit
+// functions the single-channel FP32_FIX kernels use (tiles_f32.cuh), so an item's outputs do not
+// depend on what else is in the batch.  A last kernel merges each AverageOn item's tile partials
+// with the fixed tree of hps_average_on.  Counter reset, class kernels and merge are captured
+// once into a CUDA graph; the item table and its header live in device memory, so new items need
+// no re-capture.
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -37,15 +41,21 @@ struct BatchItemDev {
     int32_t mode, N, engine, vec32;
 };
 
+// Register classes: one per N (class c holds N = c + 2).  Each class kernel carries both engines
+// and both modes of its N; ptxas gives them 60 (N = 2) to 128 (N >= 8) registers, against 128
+// for a kernel over every N.
+constexpr int kBatchClasses = 9;
+__host__ __device__ constexpr int class_lo(int c) { return c + 2; }
+__host__ __device__ constexpr int class_hi(int c) { return c + 2; }
+inline int batch_class(int N) { return N < 2 ? 0 : N > 10 ? kBatchClasses - 1 : N - 2; }
+
 struct BatchHeader {
-    unsigned long long counter;   // next work unit (reset by the graph before each launch)
-    uint64_t total_units;
+    unsigned long long counter[kBatchClasses];   // next unit of each class, relative (reset per launch)
+    uint64_t class_begin[kBatchClasses + 1];     // the units of class c are [class_begin[c], class_begin[c+1])
+    int32_t item_begin[kBatchClasses + 1];       // its items are table entries [item_begin[c], item_begin[c+1])
     int32_t n_items;
     int32_t store_tile;
 };
-
-// Largest shared-memory word exchange over N and engines (Philox, N = 10).
-constexpr int kBatchSmem = WordShare<10, kPhilox, kTileThreads>::BYTES2;
 
 template <int N, int ENGINE>
 __device__ __forceinline__ void run_unit(const BatchItemDev& it, uint64_t u, int store_tile, hps_stats* partials,
@@ -66,19 +76,28 @@ __device__ __forceinline__ void run_unit(const BatchItemDev& it, uint64_t u, int
     }
 }
 
+template <int CLS>
 __global__ void __launch_bounds__(kTileThreads)
 k_batch_f32(const BatchItemDev* __restrict__ items, BatchHeader* __restrict__ hdr, hps_stats* __restrict__ partials)
 {
-    __shared__ __align__(16) unsigned char smem[kBatchSmem];
+    // largest shared-memory word exchange of the class (Philox at its largest N)
+    __shared__ __align__(16) unsigned char smem[WordShare<class_hi(CLS), kPhilox, kTileThreads>::BYTES2];
     __shared__ unsigned long long s_unit;
     __shared__ int s_item;
-    const uint64_t total = hdr->total_units;
-    const int n_items = hdr->n_items;
+    // The unit's item, staged in shared memory: the channel constants are then re-read after the
+    // barriers of each 256-event chunk instead of being held in registers for the whole unit,
+    // which keeps the class kernels near the register counts of the single-channel kernels.
+    __shared__ __align__(16) BatchItemDev s_it;
+    static_assert(sizeof(BatchItemDev) % 8 == 0, "staged as 8-byte words");
+    const uint64_t unit_end = hdr->class_begin[CLS + 1];
+    const uint64_t unit_begin = hdr->class_begin[CLS];
+    const int item_lo = hdr->item_begin[CLS];
+    const int item_hi = hdr->item_begin[CLS + 1] - 1;
     const int store_tile = hdr->store_tile;
     for (;;) {
         if (threadIdx.x == 0) {
-            const unsigned long long u = atomicAdd(&hdr->counter, 1ull);
-            int lo = 0, hi = n_items - 1;                 // last item with unit_begin <= u
+            const unsigned long long u = unit_begin + atomicAdd(&hdr->counter[CLS], 1ull);
+            int lo = item_lo, hi = item_hi;               // last item of the class with unit_begin <= u
             while (lo < hi) {
                 const int mid = (lo + hi + 1) >> 1;
                 if (items[mid].unit_begin <= u) lo = mid; else hi = mid - 1;
@@ -88,14 +107,26 @@ k_batch_f32(const BatchItemDev* __restrict__ items, BatchHeader* __restrict__ hd
         }
         __syncthreads();
         const unsigned long long u = s_unit;
-        const BatchItemDev& it = items[s_item];
-        __syncthreads();                                  // s_unit / s_item read before they change
-        if (u >= total) return;
+        const int item = s_item;
+        if (u >= unit_end) return;                        // the whole CTA (also every class with no items)
+        {
+            const uint2* src = reinterpret_cast<const uint2*>(items + item);
+            uint2* dst = reinterpret_cast<uint2*>(&s_it);
+            for (int k = threadIdx.x; k < (int)(sizeof(BatchItemDev) / 8); k += kTileThreads) dst[k] = src[k];
+        }
+        __syncthreads();                                  // s_it staged; s_unit / s_item read before they change
+        const BatchItemDev& it = s_it;
         const uint64_t lu = u - it.unit_begin;
         switch (it.N * 2 + it.engine) {
-#define HPS_UNIT(NN)                                                                         \
-        case NN * 2 + 0: run_unit<NN, kPhilox>(it, lu, store_tile, partials, smem); break;   \
-        case NN * 2 + 1: run_unit<NN, kSquares3>(it, lu, store_tile, partials, smem); break;
+#define HPS_UNIT(NN)                                                                             \
+        case NN * 2 + 0:                                                                         \
+            if constexpr (NN >= class_lo(CLS) && NN <= class_hi(CLS))                            \
+                run_unit<NN, kPhilox>(it, lu, store_tile, partials, smem);                       \
+            break;                                                                               \
+        case NN * 2 + 1:                                                                         \
+            if constexpr (NN >= class_lo(CLS) && NN <= class_hi(CLS))                            \
+                run_unit<NN, kSquares3>(it, lu, store_tile, partials, smem);                     \
+            break;
         HPS_UNIT(2) HPS_UNIT(3) HPS_UNIT(4) HPS_UNIT(5) HPS_UNIT(6) HPS_UNIT(7) HPS_UNIT(8) HPS_UNIT(9)
         HPS_UNIT(10)
 #undef HPS_UNIT
@@ -149,6 +180,16 @@ k_batch_merge(const BatchItemDev* __restrict__ items, const BatchHeader* __restr
     if (threadIdx.x == 0) *it.stats = r;
 }
 
+typedef void (*BatchKernel)(const BatchItemDev*, BatchHeader*, hps_stats*);
+
+inline BatchKernel class_kernel(int c)
+{
+    static const BatchKernel k[kBatchClasses] = {k_batch_f32<0>, k_batch_f32<1>, k_batch_f32<2>,
+                                                 k_batch_f32<3>, k_batch_f32<4>, k_batch_f32<5>,
+                                                 k_batch_f32<6>, k_batch_f32<7>, k_batch_f32<8>};
+    return k[c];
+}
+
 }  // namespace hps
 
 using namespace hps;
@@ -159,7 +200,7 @@ struct hps_batch_plan {
     int32_t max_items = 0;
     uint64_t max_avg_tiles = 0;
     int32_t precision = HPS_PREC_FP32_FIX;
-    hps_batch_tuning tuning{2, 16384};
+    hps_batch_tuning tuning{16, 4096};    // every class kernel at the CTAs that fit; short units
     BatchItemDev* d_items = nullptr;
     BatchHeader* d_header = nullptr;
     hps_stats* d_partials = nullptr;
@@ -172,6 +213,9 @@ struct hps_batch_plan {
     uint64_t total_events = 0;
     std::vector<int> mix;              // item mix signature for the tuning cache
     cudaStream_t capture = nullptr;
+    cudaStream_t branch[kBatchClasses] = {};     // capture streams of the class kernels
+    cudaEvent_t fork = nullptr, join[kBatchClasses] = {};
+    int occupancy[kBatchClasses] = {};           // resident CTAs per SM of each class kernel
     cudaGraphExec_t exec = nullptr;
 };
 
@@ -191,13 +235,21 @@ hps_status build_graph(hps_batch_plan* p)
 {
     hps_status st = destroy_graph(p);
     if (st != HPS_OK) return st;
-    const unsigned grid = static_cast<unsigned>(p->tuning.ctas_per_sm * p->sm_count);
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamBeginCapture(p->capture, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return cuda_status(e, "cudaStreamBeginCapture");
-    cudaMemsetAsync(&p->d_header->counter, 0, sizeof(unsigned long long), p->capture);
+    cudaMemsetAsync(p->d_header->counter, 0, sizeof(p->d_header->counter), p->capture);
     k_batch_shift<<<static_cast<unsigned>(p->max_items), 32, 0, p->capture>>>(p->d_items, p->d_header);
-    k_batch_f32<<<grid, kTileThreads, 0, p->capture>>>(p->d_items, p->d_header, p->d_partials);
+    // the class kernels as parallel branches between a fork and a join
+    cudaEventRecord(p->fork, p->capture);
+    for (int c = 0; c < kBatchClasses; ++c) {
+        const int ctas = p->tuning.ctas_per_sm < p->occupancy[c] ? p->tuning.ctas_per_sm : p->occupancy[c];
+        const unsigned grid = static_cast<unsigned>((ctas > 0 ? ctas : 1) * p->sm_count);
+        cudaStreamWaitEvent(p->branch[c], p->fork, 0);
+        class_kernel(c)<<<grid, kTileThreads, 0, p->branch[c]>>>(p->d_items, p->d_header, p->d_partials);
+        cudaEventRecord(p->join[c], p->branch[c]);
+        cudaStreamWaitEvent(p->capture, p->join[c], 0);
+    }
     k_batch_merge<<<static_cast<unsigned>(p->max_items), kFinalThreads, 0, p->capture>>>(p->d_items, p->d_header,
                                                                                          p->d_partials);
     e = cudaStreamEndCapture(p->capture, &graph);
@@ -256,11 +308,25 @@ hps_status upload_items(hps_batch_plan* p, const std::vector<hps_batch_item>& it
         p->staged_pending = false;
     }
     const int n_items = static_cast<int>(items.size());
+    // table order: by register class of N, input order within a class (an N outside 2..10 is
+    // rejected below, wherever it sorts)
+    std::vector<int> order(n_items);
+    int32_t item_begin[kBatchClasses + 1] = {};
+    for (int i = 0; i < n_items; ++i) ++item_begin[batch_class(items[i].channel.n_daughters) + 1];
+    for (int c = 0; c < kBatchClasses; ++c) item_begin[c + 1] += item_begin[c];
+    {
+        int32_t next[kBatchClasses];
+        for (int c = 0; c < kBatchClasses; ++c) next[c] = item_begin[c];
+        for (int i = 0; i < n_items; ++i) order[next[batch_class(items[i].channel.n_daughters)]++] = i;
+    }
+    uint64_t class_begin[kBatchClasses + 1] = {};
     uint64_t unit = 0, partial = 0, events = 0;
     std::vector<int> mix(2 * 11 * 2, 0);
-    for (int i = 0; i < n_items; ++i) {
+    for (int pos = 0, c = 0; pos < n_items; ++pos) {
+        while (c < kBatchClasses && pos == item_begin[c + 1]) class_begin[++c] = unit;
+        const int i = order[pos];
         const hps_batch_item& in = items[i];
-        BatchItemDev& d = p->h_items[i];
+        BatchItemDev& d = p->h_items[pos];
         std::memset(&d, 0, sizeof(d));
         hps_status st = to_device_channel(&in.channel, &d.chd);
         if (st != HPS_OK) return item_error(st, i);
@@ -305,8 +371,15 @@ hps_status upload_items(hps_batch_plan* p, const std::vector<hps_batch_item>& it
         events += in.n_events;
         mix[(in.mode * 11 + N) * 2 + d.engine] += 1;
     }
-    p->h_header->counter = 0;
-    p->h_header->total_units = unit;
+    for (int c = 0; c < kBatchClasses; ++c) {
+        // classes after the last item's (and every class of an empty table) end at the last unit
+        if (item_begin[c + 1] == n_items) class_begin[c + 1] = unit;
+        p->h_header->counter[c] = 0;
+    }
+    for (int c = 0; c <= kBatchClasses; ++c) {
+        p->h_header->class_begin[c] = class_begin[c];
+        p->h_header->item_begin[c] = item_begin[c];
+    }
     p->h_header->n_items = n_items;
     p->h_header->store_tile = p->tuning.store_tile_events;
     p->n_items = n_items;
@@ -353,6 +426,13 @@ hps_status hps_batch_create(hps_batch_plan** out, int32_t max_items, uint64_t ma
     if (e == cudaSuccess) e = cudaMallocHost(&p->h_header, sizeof(BatchHeader));
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->staged, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->capture, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming);
+    for (int c = 0; c < kBatchClasses && e == cudaSuccess; ++c) {
+        e = cudaStreamCreateWithFlags(&p->branch[c], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->join[c], cudaEventDisableTiming);
+    }
+    for (int c = 0; c < kBatchClasses && e == cudaSuccess; ++c)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p->occupancy[c], class_kernel(c), kTileThreads, 0);
     if (e == cudaSuccess) e = cudaMemset(p->d_header, 0, sizeof(BatchHeader));
     if (e != cudaSuccess) {
         hps_status st = (e == cudaErrorMemoryAllocation) ? set_error(HPS_ERR_OOM, "batch plan: %s", cudaGetErrorString(e))
@@ -487,6 +567,11 @@ hps_status hps_batch_destroy(hps_batch_plan* p)
     destroy_graph(p);
     if (p->staged) { cudaEventSynchronize(p->staged); cudaEventDestroy(p->staged); }
     if (p->capture) cudaStreamDestroy(p->capture);
+    if (p->fork) cudaEventDestroy(p->fork);
+    for (int c = 0; c < kBatchClasses; ++c) {
+        if (p->branch[c]) cudaStreamDestroy(p->branch[c]);
+        if (p->join[c]) cudaEventDestroy(p->join[c]);
+    }
     if (p->d_items) cudaFree(p->d_items);
     if (p->d_header) cudaFree(p->d_header);
     if (p->d_partials) cudaFree(p->d_partials);

@@ -335,10 +335,10 @@ hps_status hps_generate_range(const hps_channel* ch, uint64_t first_evt, uint64_
 hps_status hps_rng_words(int32_t n_daughters, int32_t engine, uint64_t seed, uint64_t first_evt,
                          uint64_t n, uint64_t* out, void* stream);
 
-/* ------------------------------------------------- batched channels, one persistent launch -- */
+/* ------------------------------------------------------ batched channels, one graph launch -- */
 
-/* Many decay channels of different N and event counts in one persistent kernel (FP32_FIX
- * arithmetic).  There is no single reference call for this: it batches what would be one
+/* Many decay channels of different N and event counts in one graph launch of persistent kernels,
+ * one per N so that each runs at the occupancy of its own register count (FP32_FIX arithmetic).  There is no single reference call for this: it batches what would be one
  * PhaseSpace::Generate or AverageOn call per channel (PhaseSpace.inl:255-444).  Each item's
  * results are bit-identical to the same request made alone with hps_generate / hps_average_on
  * at HPS_PREC_FP32_FIX: the work units are the same functions of (channel, event index). */
@@ -358,9 +358,9 @@ typedef struct hps_batch_item {
     hps_stats* stats;                    /* AVERAGE: device output {mean, M2, W}             */
 } hps_batch_item;
 
-/* Launch shape of the persistent kernel: grid = ctas_per_sm x SM count CTAs of 256 threads;
- * store items are cut into work units of store_tile_events events (a multiple of 256),
- * AverageOn items into tiles of HPS_AVG_TILE events. */
+/* Launch shape of the persistent kernels: each gets min(ctas_per_sm, the CTAs of it that fit
+ * on an SM) x SM count CTAs of 256 threads; store items are cut into work units of
+ * store_tile_events events (a multiple of 256), AverageOn items into tiles of HPS_AVG_TILE events. */
 typedef struct hps_batch_tuning {
     int32_t ctas_per_sm;
     int32_t store_tile_events;
@@ -370,8 +370,8 @@ typedef struct hps_batch_plan hps_batch_plan;
 
 /* A plan owns the device item table (max_items entries), the AverageOn tile partials
  * (max_average_tiles x 24 bytes), a pinned staging copy of the table and the instantiated
- * CUDA graph (counter reset + persistent kernel + per-item merge).  tuning = NULL picks the
- * default shape; hps_batch_autotune chooses one by timing. */
+ * CUDA graph (counter reset, the per-N persistent kernels as parallel branches, per-item
+ * merge).  tuning = NULL picks the default shape; hps_batch_autotune chooses one by timing. */
 hps_status hps_batch_create(hps_batch_plan** plan, int32_t max_items, uint64_t max_average_tiles,
                             int32_t precision, const hps_batch_tuning* tuning);
 /* Validates the items and uploads the table asynchronously on `stream`. */
