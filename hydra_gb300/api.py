@@ -368,7 +368,7 @@ def average_item(ch: HpsChannel, first: int, n: int, functor: HpsFunctor, stats:
 
 
 class BatchPlan:
-    """Many channels in one persistent, graph-captured launch (hps_batch_*; FP32_FIX)."""
+    """Many channels in one graph launch of persistent kernels, one per N (hps_batch_*; FP32_FIX)."""
 
     def __init__(self, max_items: int, max_average_tiles: int, tuning: tuple[int, int] | None = None):
         self._p = ctypes.c_void_p()

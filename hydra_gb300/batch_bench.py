@@ -6,7 +6,7 @@ rest, events log-uniform in [1e3, 1e6] (about 37M in total), Philox seed 0x3039 
 (Decays columns + generation-time weight, 32N + 8 bytes per event).
 
 Compared on the same GPU:
-  batched   one graph launch of the persistent FP32_FIX kernel (hps_batch_*), autotuned shape
+  batched   one graph launch of the persistent FP32_FIX kernels, one per N (hps_batch_*), autotuned shape
   plain64   one hps_generate launch per channel, FP64 arithmetic (the reference's)
   plain32   one hps_generate launch per channel, FP32_FIX arithmetic
 Prints one JSON line.  python -m hydra_gb300.batch_bench [--channels 256] [--reps 5]

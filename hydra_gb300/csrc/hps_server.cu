@@ -1,4 +1,4 @@
-// hps_server.cu -- request server with continuous batching over the batched persistent kernel.
+// hps_server.cu -- request server with continuous batching over the batched persistent kernels.
 //
 // Host threads submit requests; one scheduler thread per server
 //   1. retires finished launches (a host callback on the stream counts completions),
