@@ -42,7 +42,7 @@ struct BatchItemDev {
 };
 
 // Register classes: one per N (class c holds N = c + 2).  Each class kernel carries both engines
-// and both modes of its N; ptxas gives them 60 (N = 2) to 128 (N >= 8) registers, against 128
+// and both modes of its N; ptxas gives them 60 (N = 2) to 128 (N = 9, 10) registers, against 128
 // for a kernel over every N.
 constexpr int kBatchClasses = 9;
 __host__ __device__ constexpr int class_lo(int c) { return c + 2; }
@@ -77,8 +77,8 @@ __device__ __forceinline__ void run_unit(const BatchItemDev& it, uint64_t u, int
 }
 
 template <int CLS>
-__global__ void __launch_bounds__(kTileThreads)
-k_batch_f32(const BatchItemDev* __restrict__ items, BatchHeader* __restrict__ hdr, hps_stats* __restrict__ partials)
+__device__ __forceinline__ void batch_body(const BatchItemDev* __restrict__ items, BatchHeader* __restrict__ hdr,
+                                           hps_stats* __restrict__ partials)
 {
     // largest shared-memory word exchange of the class (Philox at its largest N)
     __shared__ __align__(16) unsigned char smem[WordShare<class_hi(CLS), kPhilox, kTileThreads>::BYTES2];
@@ -135,6 +135,22 @@ k_batch_f32(const BatchItemDev* __restrict__ items, BatchHeader* __restrict__ hd
     }
 }
 
+template <int CLS>
+__global__ void __launch_bounds__(kTileThreads)
+k_batch_f32(const BatchItemDev* __restrict__ items, BatchHeader* __restrict__ hdr, hps_stats* __restrict__ partials)
+{
+    batch_body<CLS>(items, hdr, partials);
+}
+
+// N = 7 and 8 capped at 80 registers (3 CTAs per SM instead of 2, a few bytes of spill):
+// 0.74 / 0.90 ms against 0.81 / 0.95 ms for one 2^23-event channel in the batch.
+template <int CLS>
+__global__ void __launch_bounds__(kTileThreads, 3)
+k_batch_f32_3(const BatchItemDev* __restrict__ items, BatchHeader* __restrict__ hdr, hps_stats* __restrict__ partials)
+{
+    batch_body<CLS>(items, hdr, partials);
+}
+
 // One CTA per item slot: the shift K0 of each AverageOn item into the first 4 bytes of its stats
 // output, as k_shift_f32 does for hps_average_on.
 __global__ void k_batch_shift(const BatchItemDev* __restrict__ items, const BatchHeader* __restrict__ hdr)
@@ -185,8 +201,8 @@ typedef void (*BatchKernel)(const BatchItemDev*, BatchHeader*, hps_stats*);
 inline BatchKernel class_kernel(int c)
 {
     static const BatchKernel k[kBatchClasses] = {k_batch_f32<0>, k_batch_f32<1>, k_batch_f32<2>,
-                                                 k_batch_f32<3>, k_batch_f32<4>, k_batch_f32<5>,
-                                                 k_batch_f32<6>, k_batch_f32<7>, k_batch_f32<8>};
+                                                 k_batch_f32<3>, k_batch_f32<4>, k_batch_f32_3<5>,
+                                                 k_batch_f32_3<6>, k_batch_f32<7>, k_batch_f32<8>};
     return k[c];
 }
 
