@@ -9,7 +9,7 @@ Compared on the same GPU:
   batched   one graph launch of the persistent FP32_FIX kernels, one per N (hps_batch_*), autotuned shape
   plain64   one hps_generate launch per channel, FP64 arithmetic (the reference's)
   plain32   one hps_generate launch per channel, FP32_FIX arithmetic
-Prints one JSON line.  python -m hydra_gb300.batch_bench [--channels 256] [--reps 5]
+Prints one JSON line.  python -m hydra_gb300.batch_bench [--channels 256] [--reps 5] [--tuning C,T]
 """
 from __future__ import annotations
 
@@ -58,6 +58,7 @@ def main(argv=None):
     ap.add_argument("--channels", type=int, default=256)
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--tune-cache", default=None)
+    ap.add_argument("--tuning", default=None, help="CTAS_PER_SM,STORE_TILE instead of autotuning")
     args = ap.parse_args(argv)
     import torch
     from hydra_gb300 import api
@@ -78,7 +79,12 @@ def main(argv=None):
 
     plan = api.BatchPlan(len(items), 1)
     plan.set_items(items)
-    tuning = plan.autotune(args.tune_cache)
+    if args.tuning:
+        c, t = (int(x) for x in args.tuning.split(","))
+        plan.set_tuning(c, t)
+        tuning = plan.tuning()
+    else:
+        tuning = plan.autotune(args.tune_cache)
     t_batch = timed(plan.launch, torch, args.reps)
 
     def plain(prec):

@@ -167,3 +167,23 @@ def test_batch_rejects_bad_item(api, torch, hps):
     with pytest.raises(hps.HpsError, match="exceed"):
         plan.set_items([big])
     plan.close()
+
+
+def test_batch_single_class_empty_and_reordered(api, torch):
+    """Items of one N only (the other per-N kernels find no work), an empty item list, and a
+    mix given in descending N (the table is reordered by N): every item equals its call alone."""
+    mix = [r for r in make_mix(api, torch, 60, seed=4) if r[1].n_daughters == 5][:4]
+    assert mix
+    plan = api.BatchPlan(32, 512)
+    plan.set_items(items_of(api, mix))
+    plan.launch()
+    assert_same_as_alone(api, torch, mix)
+    plan.set_items([])
+    plan.launch()
+    torch.cuda.synchronize()
+    mix2 = sorted(make_mix(api, torch, 16, seed=5, n_lo=500, n_hi=5e4), key=lambda r: -r[1].n_daughters)
+    assert sum((r[3] + 4095) // 4096 for r in mix2 if r[0] == "avg") <= 512
+    plan.set_items(items_of(api, mix2))
+    plan.launch()
+    assert_same_as_alone(api, torch, mix2)
+    plan.close()
