@@ -7,7 +7,10 @@ uses, and launches its kernels on torch's current stream:
 * ``generate``   -- hydra::detail::DecayMother::operator()(evt) per event, the N
   Vector4R it returns stored as N columns (the Decays layout), as Generate does;
 * ``average_bw`` -- hydra::detail::AverageMother::operator()(evt) with the
-  Breit-Wigner |BW(m_ij)|^2 functor, folded with AddStatsPHSP, as AverageOn does.
+  Breit-Wigner |BW(m_ij)|^2 functor, folded with AddStatsPHSP, as AverageOn does;
+* ``evaluate`` -- hydra::detail::EvalMother (Evaluate) with |BW|^2 and m^2 functors;
+* ``generate_mothers`` / ``average_mothers_bw`` -- DecayMothers / AverageMothers with one
+  mother per event.
 
 The tests use it to check the product against the reference's own CUDA arithmetic;
 ``python oracle/ref_gpu.py`` times it on the GPU at the benchmark workloads and prints
@@ -43,6 +46,14 @@ def _mother_args(n: int):
 
 class _BW(ctypes.Structure):
     _fields_ = [("i", ctypes.c_int32), ("j", ctypes.c_int32), ("a", ctypes.c_double), ("b", ctypes.c_double)]
+
+
+@functools.lru_cache(maxsize=None)
+def _mothers_args(n: int):
+    class MothersArgs(ctypes.Structure):
+        _fields_ = [("seed", ctypes.c_uint64), ("ecm", ctypes.c_double), ("maxw", ctypes.c_double),
+                    ("masses", ctypes.c_double * n)]
+    return MothersArgs
 
 
 _state = {}
@@ -119,6 +130,60 @@ def generate(ch, first: int, n: int, out=None):
                 [_args(ch), ctypes.c_uint64(first), ctypes.c_uint64(n), ctypes.c_void_p(cols.data_ptr())])
     out._ref_cols = cols            # the pointer array must outlive the launch
     return out
+
+
+def _margs(ch):
+    n = ch.n_daughters
+    a = _mothers_args(n)()
+    a.seed = ch.seed
+    a.ecm = ch.ecm
+    a.maxw = ch.max_weight
+    for k in range(n):
+        a.masses[k] = ch.masses[k]
+    return a
+
+
+def _grid(n: int) -> int:
+    return max(1, (n + THREADS - 1) // THREADS)
+
+
+def evaluate(ch, first: int, n: int, bw=(0, 1, 0.8955, 0.0473), m2=(0, 1)):
+    """The reference's EvalMother with two functors, |BW(m_ij)|^2 and m^2(p_k + p_l): float64
+    cuda tensors (weight, bw, m2) of n events each."""
+    import torch
+    w, fb, fm = (torch.empty(n, dtype=torch.float64, device="cuda") for _ in range(3))
+    if n:
+        _launch(f"ref_evaluate_{ch.n_daughters}_{ENGINES[ch.engine]}", _grid(n),
+                [_args(ch), _BW(*bw), _BW(m2[0], m2[1], 0.0, 0.0), ctypes.c_uint64(first), ctypes.c_uint64(n),
+                 ctypes.c_void_p(w.data_ptr()), ctypes.c_void_p(fb.data_ptr()), ctypes.c_void_p(fm.data_ptr())])
+    return w, fb, fm
+
+
+def generate_mothers(ch, first: int, mothers):
+    """The reference's DecayMothers: mothers is a float64 (n, 4) cuda tensor; returns (N, n, 4)."""
+    import torch
+    N, n = ch.n_daughters, mothers.shape[0]
+    out = torch.empty((N, n, 4), dtype=torch.float64, device="cuda")
+    cols = torch.tensor([out[i].data_ptr() for i in range(N)], dtype=torch.int64, device="cuda")
+    if n:
+        _launch(f"ref_generate_mothers_{N}_{ENGINES[ch.engine]}", _grid(n),
+                [_margs(ch), ctypes.c_uint64(first), ctypes.c_uint64(n), ctypes.c_void_p(mothers.data_ptr()),
+                 ctypes.c_void_p(cols.data_ptr())])
+    out._ref_cols = cols
+    return out
+
+
+def average_mothers_bw(ch, i: int, j: int, a: float, b: float, first: int, mothers):
+    """The reference's AverageMothers with |BW(m_ij)|^2 (indices count the mother as 0);
+    returns (mean, sqrt(M2)/W)."""
+    import torch
+    n = mothers.shape[0]
+    grid = max(1, min(_grid(n), AVG_BLOCKS))
+    partial = torch.empty((grid, 3), dtype=torch.float64, device="cuda")
+    _launch(f"ref_average_mothers_bw_{ch.n_daughters}_{ENGINES[ch.engine]}", grid,
+            [_margs(ch), _BW(i, j, a, b), ctypes.c_uint64(first), ctypes.c_uint64(n),
+             ctypes.c_void_p(mothers.data_ptr()), ctypes.c_void_p(partial.data_ptr())])
+    return fold(partial)
 
 
 def add_stats(x, y):

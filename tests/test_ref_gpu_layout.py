@@ -31,3 +31,11 @@ def test_add_stats_matches_definition():
     mean, m2, w = ref_gpu.add_stats(x, y)
     assert w == 4.0 and mean == (2.0 * 3.0 + 4.0 * 1.0) / 4.0
     assert m2 == 0.5 + 0.25 + 4.0 * 3.0 * 1.0 / 4.0
+
+
+@pytest.mark.parametrize("n", range(2, 11))
+def test_mothers_args_layout(n):
+    # MothersArgs<N> = {size_t seed; double ecm, maxw, masses[N]} (DecayMothers.h:59-63)
+    M = ref_gpu._mothers_args(n)
+    assert ctypes.sizeof(M) == 8 * (3 + n)
+    assert M.masses.offset == 24
