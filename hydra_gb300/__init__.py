@@ -85,8 +85,13 @@ class HpsBatchItem(ctypes.Structure):
     ]
 
 
+BATCH_PER_N = 0          # hps_batch_form: one persistent kernel per N, parallel graph branches
+BATCH_ONE_KERNEL = 1     # one persistent kernel over every N
+
+
 class HpsBatchTuning(ctypes.Structure):
-    _fields_ = [("ctas_per_sm", ctypes.c_int32), ("store_tile_events", ctypes.c_int32)]
+    _fields_ = [("ctas_per_sm", ctypes.c_int32), ("store_tile_events", ctypes.c_int32),
+                ("kernel_form", ctypes.c_int32)]
 
 
 MODE_STORE, MODE_AVERAGE = 0, 1

@@ -9,7 +9,7 @@ Compared on the same GPU:
   batched   one graph launch of the persistent FP32_FIX kernels, one per N (hps_batch_*), autotuned shape
   plain64   one hps_generate launch per channel, FP64 arithmetic (the reference's)
   plain32   one hps_generate launch per channel, FP32_FIX arithmetic
-Prints one JSON line.  python -m hydra_gb300.batch_bench [--channels 256] [--reps 5] [--tuning C,T]
+Prints one JSON line.  python -m hydra_gb300.batch_bench [--channels 256] [--reps 5] [--tuning C,T[,FORM]]
 """
 from __future__ import annotations
 
@@ -58,7 +58,7 @@ def main(argv=None):
     ap.add_argument("--channels", type=int, default=256)
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--tune-cache", default=None)
-    ap.add_argument("--tuning", default=None, help="CTAS_PER_SM,STORE_TILE instead of autotuning")
+    ap.add_argument("--tuning", default=None, help="CTAS_PER_SM,STORE_TILE[,FORM] instead of autotuning")
     args = ap.parse_args(argv)
     import torch
     from hydra_gb300 import api
@@ -80,8 +80,7 @@ def main(argv=None):
     plan = api.BatchPlan(len(items), 1)
     plan.set_items(items)
     if args.tuning:
-        c, t = (int(x) for x in args.tuning.split(","))
-        plan.set_tuning(c, t)
+        plan.set_tuning(*(int(x) for x in args.tuning.split(",")))
         tuning = plan.tuning()
     else:
         tuning = plan.autotune(args.tune_cache)
@@ -117,7 +116,8 @@ def main(argv=None):
         "events": total, "bytes": nbytes,
         "batched": {"ms": t_batch, "events_per_s": total / (t_batch / 1e3), "gbs": gbs,
                     "hbm_frac": (gbs / peak) if peak else None, "tuning": {"ctas_per_sm": tuning[0],
-                                                                           "store_tile_events": tuning[1]}},
+                                                                           "store_tile_events": tuning[1],
+                                                                           "kernel_form": ["per_N", "one_kernel"][tuning[2]]}},
         "plain_fp64_per_channel": {"ms": t_plain64, "events_per_s": total / (t_plain64 / 1e3)},
         "plain_fp32fix_per_channel": {"ms": t_plain32, "events_per_s": total / (t_plain32 / 1e3)},
         "speedup_vs_plain_fp64": t_plain64 / t_batch,

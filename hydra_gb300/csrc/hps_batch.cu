@@ -50,7 +50,9 @@ __host__ __device__ constexpr int class_hi(int c) { return c + 2; }
 inline int batch_class(int N) { return N < 2 ? 0 : N > 10 ? kBatchClasses - 1 : N - 2; }
 
 struct BatchHeader {
-    unsigned long long counter[kBatchClasses];   // next unit of each class, relative (reset per launch)
+    // next unit of each class, relative; the last one serves the single kernel over every N
+    // (reset per launch)
+    unsigned long long counter[kBatchClasses + 1];
     uint64_t class_begin[kBatchClasses + 1];     // the units of class c are [class_begin[c], class_begin[c+1])
     int32_t item_begin[kBatchClasses + 1];       // its items are table entries [item_begin[c], item_begin[c+1])
     int32_t n_items;
@@ -151,6 +153,49 @@ k_batch_f32_3(const BatchItemDev* __restrict__ items, BatchHeader* __restrict__ 
     batch_body<CLS>(items, hdr, partials);
 }
 
+// The single-kernel form (hps_batch_tuning.kernel_form = HPS_BATCH_ONE_KERNEL): one persistent
+// kernel takes every unit of every N from one counter and dispatches on N, reading the item from
+// global memory.  Its register count is that of the largest N for all of them.
+__global__ void __launch_bounds__(kTileThreads)
+k_batch_f32_all(const BatchItemDev* __restrict__ items, BatchHeader* __restrict__ hdr,
+                hps_stats* __restrict__ partials)
+{
+    __shared__ __align__(16) unsigned char smem[WordShare<10, kPhilox, kTileThreads>::BYTES2];
+    __shared__ unsigned long long s_unit;
+    __shared__ int s_item;
+    const uint64_t total = hdr->class_begin[kBatchClasses];
+    const int n_items = hdr->n_items;
+    const int store_tile = hdr->store_tile;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const unsigned long long u = atomicAdd(&hdr->counter[kBatchClasses], 1ull);
+            int lo = 0, hi = n_items - 1;                 // last item with unit_begin <= u
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (items[mid].unit_begin <= u) lo = mid; else hi = mid - 1;
+            }
+            s_unit = u;
+            s_item = lo;
+        }
+        __syncthreads();
+        const unsigned long long u = s_unit;
+        const int item = s_item;
+        __syncthreads();                                  // s_unit / s_item read before they change
+        if (u >= total) return;
+        const BatchItemDev& it = items[item];
+        const uint64_t lu = u - it.unit_begin;
+        switch (it.N * 2 + it.engine) {
+#define HPS_UNIT(NN)                                                                         \
+        case NN * 2 + 0: run_unit<NN, kPhilox>(it, lu, store_tile, partials, smem); break;   \
+        case NN * 2 + 1: run_unit<NN, kSquares3>(it, lu, store_tile, partials, smem); break;
+        HPS_UNIT(2) HPS_UNIT(3) HPS_UNIT(4) HPS_UNIT(5) HPS_UNIT(6) HPS_UNIT(7) HPS_UNIT(8) HPS_UNIT(9)
+        HPS_UNIT(10)
+#undef HPS_UNIT
+        default: break;
+        }
+    }
+}
+
 // One CTA per item slot: the shift K0 of each AverageOn item into the first 4 bytes of its stats
 // output, as k_shift_f32 does for hps_average_on.
 __global__ void k_batch_shift(const BatchItemDev* __restrict__ items, const BatchHeader* __restrict__ hdr)
@@ -216,7 +261,7 @@ struct hps_batch_plan {
     int32_t max_items = 0;
     uint64_t max_avg_tiles = 0;
     int32_t precision = HPS_PREC_FP32_FIX;
-    hps_batch_tuning tuning{16, 4096};    // every class kernel at the CTAs that fit; short units
+    hps_batch_tuning tuning{16, 4096, HPS_BATCH_PER_N};   // every kernel at the CTAs that fit; short units
     BatchItemDev* d_items = nullptr;
     BatchHeader* d_header = nullptr;
     hps_stats* d_partials = nullptr;
@@ -231,7 +276,8 @@ struct hps_batch_plan {
     cudaStream_t capture = nullptr;
     cudaStream_t branch[kBatchClasses] = {};     // capture streams of the class kernels
     cudaEvent_t fork = nullptr, join[kBatchClasses] = {};
-    int occupancy[kBatchClasses] = {};           // resident CTAs per SM of each class kernel
+    int occupancy[kBatchClasses + 1] = {};       // resident CTAs per SM of each class kernel, then of
+                                                 // the single kernel over every N
     cudaGraphExec_t exec = nullptr;
 };
 
@@ -256,15 +302,22 @@ hps_status build_graph(hps_batch_plan* p)
     if (e != cudaSuccess) return cuda_status(e, "cudaStreamBeginCapture");
     cudaMemsetAsync(p->d_header->counter, 0, sizeof(p->d_header->counter), p->capture);
     k_batch_shift<<<static_cast<unsigned>(p->max_items), 32, 0, p->capture>>>(p->d_items, p->d_header);
-    // the class kernels as parallel branches between a fork and a join
-    cudaEventRecord(p->fork, p->capture);
-    for (int c = 0; c < kBatchClasses; ++c) {
+    auto grid_of = [p](int c) {
         const int ctas = p->tuning.ctas_per_sm < p->occupancy[c] ? p->tuning.ctas_per_sm : p->occupancy[c];
-        const unsigned grid = static_cast<unsigned>((ctas > 0 ? ctas : 1) * p->sm_count);
-        cudaStreamWaitEvent(p->branch[c], p->fork, 0);
-        class_kernel(c)<<<grid, kTileThreads, 0, p->branch[c]>>>(p->d_items, p->d_header, p->d_partials);
-        cudaEventRecord(p->join[c], p->branch[c]);
-        cudaStreamWaitEvent(p->capture, p->join[c], 0);
+        return static_cast<unsigned>((ctas > 0 ? ctas : 1) * p->sm_count);
+    };
+    if (p->tuning.kernel_form == HPS_BATCH_ONE_KERNEL) {
+        k_batch_f32_all<<<grid_of(kBatchClasses), kTileThreads, 0, p->capture>>>(p->d_items, p->d_header,
+                                                                                 p->d_partials);
+    } else {
+        // the class kernels as parallel branches between a fork and a join
+        cudaEventRecord(p->fork, p->capture);
+        for (int c = 0; c < kBatchClasses; ++c) {
+            cudaStreamWaitEvent(p->branch[c], p->fork, 0);
+            class_kernel(c)<<<grid_of(c), kTileThreads, 0, p->branch[c]>>>(p->d_items, p->d_header, p->d_partials);
+            cudaEventRecord(p->join[c], p->branch[c]);
+            cudaStreamWaitEvent(p->capture, p->join[c], 0);
+        }
     }
     k_batch_merge<<<static_cast<unsigned>(p->max_items), kFinalThreads, 0, p->capture>>>(p->d_items, p->d_header,
                                                                                          p->d_partials);
@@ -287,6 +340,9 @@ hps_status check_tuning(const hps_batch_tuning* t)
         t->store_tile_events > (1 << 24))
         return set_error(HPS_ERR_BAD_ARG, "store_tile_events %d not a multiple of 256 in 256..2^24",
                          t->store_tile_events);
+    if (t->kernel_form != HPS_BATCH_PER_N && t->kernel_form != HPS_BATCH_ONE_KERNEL)
+        return set_error(HPS_ERR_BAD_ARG, "kernel_form %d is neither HPS_BATCH_PER_N nor HPS_BATCH_ONE_KERNEL",
+                         t->kernel_form);
     return HPS_OK;
 }
 
@@ -449,6 +505,9 @@ hps_status hps_batch_create(hps_batch_plan** out, int32_t max_items, uint64_t ma
     }
     for (int c = 0; c < kBatchClasses && e == cudaSuccess; ++c)
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p->occupancy[c], class_kernel(c), kTileThreads, 0);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p->occupancy[kBatchClasses], k_batch_f32_all,
+                                                          kTileThreads, 0);
     if (e == cudaSuccess) e = cudaMemset(p->d_header, 0, sizeof(BatchHeader));
     if (e != cudaSuccess) {
         hps_status st = (e == cudaErrorMemoryAllocation) ? set_error(HPS_ERR_OOM, "batch plan: %s", cudaGetErrorString(e))
@@ -532,7 +591,8 @@ hps_status hps_batch_autotune(hps_batch_plan* p, void* stream, const char* cache
             std::string k;
             hps_batch_tuning t;
             double ms;
-            if ((ls >> k >> t.ctas_per_sm >> t.store_tile_events >> ms) && k == key && check_tuning(&t) == HPS_OK) {
+            if ((ls >> k >> t.ctas_per_sm >> t.store_tile_events >> t.kernel_form >> ms) && k == key &&
+                check_tuning(&t) == HPS_OK) {
                 hps_status st = hps_batch_set_tuning(p, &t);
                 if (st == HPS_OK && chosen) *chosen = t;
                 return st;
@@ -546,8 +606,9 @@ hps_status hps_batch_autotune(hps_batch_plan* p, void* stream, const char* cache
     const int ctas[] = {1, 2, 3, 4, 6, 8};
     const int tiles[] = {4096, 16384, 65536};
     std::vector<hps_batch_tuning> cands;
-    for (int tile : tiles)
-        for (int c : ctas) cands.push_back(hps_batch_tuning{c, tile});
+    for (int form : {HPS_BATCH_PER_N, HPS_BATCH_ONE_KERNEL})
+        for (int tile : tiles)
+            for (int c : ctas) cands.push_back(hps_batch_tuning{c, tile, form});
     hps_batch_tuning best = p->tuning;
     float best_ms = 1e30f;
     hps_status st = HPS_OK;
@@ -571,7 +632,8 @@ hps_status hps_batch_autotune(hps_batch_plan* p, void* stream, const char* cache
     if (cache_path) {
         std::lock_guard<std::mutex> lock(cache_mu);
         std::ofstream outf(cache_path, std::ios::app);
-        outf << key << " " << best.ctas_per_sm << " " << best.store_tile_events << " " << best_ms / 3.0f << "\n";
+        outf << key << " " << best.ctas_per_sm << " " << best.store_tile_events << " " << best.kernel_form << " "
+             << best_ms / 3.0f << "\n";
     }
     if (chosen) *chosen = best;
     return HPS_OK;

@@ -39,7 +39,7 @@ extern "C" {
 #endif
 
 #define HPS_MAX_DAUGHTERS 10
-#define HPS_ABI_VERSION 1
+#define HPS_ABI_VERSION 2
 
 typedef enum hps_status {
     HPS_OK = 0,
@@ -337,9 +337,11 @@ hps_status hps_rng_words(int32_t n_daughters, int32_t engine, uint64_t seed, uin
 
 /* ------------------------------------------------------ batched channels, one graph launch -- */
 
-/* Many decay channels of different N and event counts in one graph launch of persistent kernels,
- * one per N so that each runs at the occupancy of its own register count (FP32_FIX arithmetic).  There is no single reference call for this: it batches what would be one
- * PhaseSpace::Generate or AverageOn call per channel (PhaseSpace.inl:255-444).  Each item's
+/* Many decay channels of different N and event counts in one graph launch of persistent kernels
+ * (FP32_FIX arithmetic): one per N, so that each runs at the occupancy of its own register count,
+ * or one over every N (hps_batch_tuning.kernel_form; the autotuner tries both).  There is no
+ * single reference call for this: it batches what would be one PhaseSpace::Generate or AverageOn
+ * call per channel (PhaseSpace.inl:255-444).  Each item's
  * results are bit-identical to the same request made alone with hps_generate / hps_average_on
  * at HPS_PREC_FP32_FIX: the work units are the same functions of (channel, event index). */
 typedef enum hps_batch_mode { HPS_MODE_STORE = 0, HPS_MODE_AVERAGE = 1 } hps_batch_mode;
@@ -360,18 +362,25 @@ typedef struct hps_batch_item {
 
 /* Launch shape of the persistent kernels: each gets min(ctas_per_sm, the CTAs of it that fit
  * on an SM) x SM count CTAs of 256 threads; store items are cut into work units of
- * store_tile_events events (a multiple of 256), AverageOn items into tiles of HPS_AVG_TILE events. */
+ * store_tile_events events (a multiple of 256), AverageOn items into tiles of HPS_AVG_TILE events.
+ * kernel_form: HPS_BATCH_PER_N runs one persistent kernel per N as parallel branches of the
+ * graph, each at the occupancy of its own register count; HPS_BATCH_ONE_KERNEL runs one
+ * persistent kernel over every N (the register count of N = 10 for all).  Each thread owns one
+ * event in both forms (its kinematics stay in that thread's registers; the random words of a
+ * CTA's events are computed cooperatively).  Results do not depend on the shape. */
+typedef enum hps_batch_form { HPS_BATCH_PER_N = 0, HPS_BATCH_ONE_KERNEL = 1 } hps_batch_form;
+
 typedef struct hps_batch_tuning {
     int32_t ctas_per_sm;
     int32_t store_tile_events;
+    int32_t kernel_form;                 /* hps_batch_form */
 } hps_batch_tuning;
 
 typedef struct hps_batch_plan hps_batch_plan;
 
 /* A plan owns the device item table (max_items entries), the AverageOn tile partials
  * (max_average_tiles x 24 bytes), a pinned staging copy of the table and the instantiated
- * CUDA graph (counter reset, the per-N persistent kernels as parallel branches, per-item
- * merge).  tuning = NULL picks the default shape; hps_batch_autotune chooses one by timing. */
+ * CUDA graph (counter reset, the persistent kernel(s), per-item merge).  tuning = NULL picks the default shape; hps_batch_autotune chooses one by timing. */
 hps_status hps_batch_create(hps_batch_plan** plan, int32_t max_items, uint64_t max_average_tiles,
                             int32_t precision, const hps_batch_tuning* tuning);
 /* Validates the items and uploads the table asynchronously on `stream`. */
