@@ -1,0 +1,88 @@
+"""One entry point on one channel, timed alone: Generate, AverageOn or Evaluate.
+
+Channels (Philox, seed 0x3039, mother at rest):
+  3    B0 -> J/psi K pi       M = 5.27934, m = (3.0969, 0.493677, 0.13957)
+  5    D0 -> K pi pi pi pi    M = 1.86484, m = (0.493677, 0.13957 x 4)
+  10   ten pions             M = 5.0,     m = 0.13957 x 10
+The functor of AverageOn and Evaluate is |BW(m_01)|^2 (m0 = 0.8955, G0 = 0.0473); Evaluate
+stores the generation-time weight and the functor value (16 bytes per event), Generate the
+Decays columns, the weight and the unweight flag (32N + 9 bytes per event).
+
+Prints one JSON line: ms per call (CUDA events, mean of --steps calls after --warmup), events/s
+and, for the storing forms, the GB/s of algorithmic bytes written.
+
+    python -m hydra_gb300.kernel_bench --op evaluate --n-daughters 5 --events 16777216 --precision fp32_fix
+"""
+from __future__ import annotations
+
+import argparse
+import json
+
+CHANNELS = {
+    3: (5.27934, [3.0969, 0.493677, 0.13957]),
+    5: (1.86484, [0.493677] + [0.13957] * 4),
+    10: (5.0, [0.13957] * 10),
+}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--op", choices=["generate", "average", "evaluate"], default="evaluate")
+    ap.add_argument("--n-daughters", type=int, choices=sorted(CHANNELS), default=5)
+    ap.add_argument("--events", type=int, default=1 << 24)
+    ap.add_argument("--precision", choices=["fp64", "fp32_fix"], default="fp32_fix")
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    args = ap.parse_args(argv)
+    import torch
+    from hydra_gb300 import api
+
+    N, n = args.n_daughters, args.events
+    M, masses = CHANNELS[N]
+    ch = api.make_channel(masses, M, 0x3039, "philox")
+    fn = api.functor_bw2(0, 1, 0.8955, 0.0473)
+    dev = "cuda"
+    stored = 0
+    if args.op == "generate":
+        four = torch.empty((N, n, 4), dtype=torch.float64, device=dev)
+        w = torch.empty(n, dtype=torch.float64, device=dev)
+        fl = torch.empty(n, dtype=torch.uint8, device=dev)
+        stored = n * (32 * N + 9)
+
+        def step():
+            api.generate(ch, 0, four, w, fl, precision=args.precision)
+    elif args.op == "average":
+        out = torch.empty(3, dtype=torch.float64, device=dev)
+        ws = torch.empty(api.average_on_workspace_size(n), dtype=torch.uint8, device=dev)
+
+        def step():
+            api.average_on(ch, 0, n, fn, out, ws, precision=args.precision)
+    else:
+        w = torch.empty(n, dtype=torch.float64, device=dev)
+        f = torch.empty(n, dtype=torch.float64, device=dev)
+        stored = n * 16
+
+        def step():
+            api.evaluate(ch, 0, n, [fn], w, [f], precision=args.precision)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(args.steps):
+        step()
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / args.steps
+    line = {"op": args.op, "n_daughters": N, "events": n, "precision": args.precision, "ms": ms,
+            "events_per_s": n / ms * 1e3}
+    if stored:
+        line["stored_gbs"] = stored / ms / 1e6
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
