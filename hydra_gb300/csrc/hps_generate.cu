@@ -41,16 +41,24 @@ k_generate_f64(DevChannel ch, Cols cols, double* __restrict__ weights, uint8_t* 
 // generation-time weight.
 constexpr int kGenThreads = kTileThreads;
 
+// CTA size of the store kernel.  Smaller CTAs wait less at the per-chunk barrier of the shared
+// random words (at the cost of (B - 1) / NT more Philox blocks per event): at N = 5, 2^24 events,
+// 128 threads took 0.622 ms against 0.633 ms for 256 and 0.667 ms for 64.  With the float-float
+// weight (N >= 7) 256 threads are faster (N = 7: 1.31 ms against 1.39 ms; N = 10 at 2^26
+// events: 9.54 ms against 10.9 ms).
+__host__ __device__ constexpr int gen_threads(int N) { return N <= 6 ? 128 : kGenThreads; }
+
 template <int N, int ENGINE>
-__global__ void __launch_bounds__(kGenThreads)
+__global__ void __launch_bounds__(gen_threads(N))
 k_generate_f32fix(DevChannel chd, DevChannelF ch, Cols cols, double* __restrict__ weights,
                   uint8_t* __restrict__ flags, uint64_t ukey, uint64_t first, uint64_t n, int vec32)
 {
-    __shared__ __align__(16) unsigned char smem[WordShare<N, ENGINE, kGenThreads>::BYTES2];
-    const uint64_t step = (uint64_t)gridDim.x * kGenThreads;
+    constexpr int NT = gen_threads(N);
+    __shared__ __align__(16) unsigned char smem[WordShare<N, ENGINE, NT>::BYTES2];
+    const uint64_t step = (uint64_t)gridDim.x * NT;
     int parity = 0;
-    for (uint64_t cb = (uint64_t)blockIdx.x * kGenThreads; cb < n; cb += step, parity ^= 1)
-        store_chunk_f32<N, ENGINE>(chd, ch, cols, weights, flags, ukey, first, n, cb, vec32 != 0, smem, parity);
+    for (uint64_t cb = (uint64_t)blockIdx.x * NT; cb < n; cb += step, parity ^= 1)
+        store_chunk_f32<N, ENGINE, NT>(chd, ch, cols, weights, flags, ukey, first, n, cb, vec32 != 0, smem, parity);
 }
 
 constexpr int kMaxFunctors = 8;
@@ -128,7 +136,7 @@ hps_status hps_generate(const hps_channel* channel, uint64_t first_evt, uint64_t
         DevChannelF chf;
         to_device_channel_f(channel, &chf);
 #define HPS_BODY(NN, EE)                                                                         \
-        k_generate_f32fix<NN, EE><<<grid, kGenThreads, 0, as_stream(stream)>>>(ch, chf, cc, weights, flags, ukey, \
+        k_generate_f32fix<NN, EE><<<grid_for(n, gen_threads(NN), 152u * 64u), gen_threads(NN), 0, as_stream(stream)>>>(ch, chf, cc, weights, flags, ukey, \
                                                                         first_evt, n, vec32);
         HPS_DISPATCH_N_ENGINE(N, channel->engine, HPS_BODY)
 #undef HPS_BODY
