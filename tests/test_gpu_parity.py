@@ -5,7 +5,7 @@ Bars (FP64 form):
     bit-exact (every operation on their path is a correctly rounded IEEE operation
     issued in the reference's order);
   * four-vectors and functor values: max_k |dp_k| / E <= 1e-12 per daughter, the
-    energy-normalised error of the spec contract (only cos/sin of the azimuth
+    energy-normalised error of the precision contract (only cos/sin of the azimuth
     may differ in the last bit between CUDA and the host libm);
   * AverageOn: mean and M2 agree with the oracle's sequential fold to 1e-10 relative
     (same events, different merge order) and the mean agrees with the reference
