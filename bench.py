@@ -57,7 +57,7 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-DEFAULT_N = 1 << 24          # events per step of the bench workload (config 2)
+DEFAULT_N = 1 << 24          # events per step of the D0 -> K pi pi pi pi bench workload
 
 
 def profiled_traffic(precision):

@@ -1,15 +1,16 @@
 """Store-path measurements of the single-channel workloads other than the bench line.
 
-  config 1   N=3, M=5.27934 at rest, m=(3.0969, 0.493677, 0.13957), 10^6 events, Philox seed 0x3039:
-             Decays + weight (104 B/event), FP64 and FP32_FIX
-  config 3   the config-1 channel and a 10-body decay (M=5.0, 10 x 0.13957) at 2^26 events each,
-             FP32_FIX (104 and 328 B/event); the maximum error of every output against the FP64
-             form of the same events is taken over ALL 2^26 events (the FP64 kernels follow the
-             reference's arithmetic operation for operation)
+  b0_1e6        B0 -> J/psi K pi: N=3, M=5.27934 at rest, m=(3.0969, 0.493677, 0.13957), 10^6
+                events, Philox seed 0x3039: Decays + weight (104 B/event), FP64 and FP32_FIX
+  b0_2e26       the same channel at 2^26 events
+  pions10_2e26  ten pions from M=5.0 (10 x 0.13957) at 2^26 events (328 B/event)
+For each, FP64 and FP32_FIX; at 2^26 events the maximum error of every FP32_FIX output against
+the FP64 form of the same events is taken over ALL events (the FP64 kernels follow the
+reference's arithmetic operation for operation).
 
 Each line: kernel time (median of --reps CUDA-event timings after a warm-up), events/s, achieved
 GB/s of algorithmic bytes against the measured HBM copy peak, and for FP32_FIX the max errors.
-python -m hydra_gb300.config_bench [--reps 5] [--configs 1,3]
+python -m hydra_gb300.config_bench [--reps 5] [--workloads b0_1e6,b0_2e26,pions10_2e26]
 """
 from __future__ import annotations
 
@@ -87,22 +88,22 @@ def run_case(api, torch, name, masses, M, n, precisions, reps, peak, check):
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--reps", type=int, default=5)
-    ap.add_argument("--configs", default="1,3")
+    ap.add_argument("--workloads", default="b0_1e6,b0_2e26,pions10_2e26")
     args = ap.parse_args(argv)
     sys.path.insert(0, str(Path(__file__).resolve().parent.parent))
     import torch
     from hydra_gb300 import api
     peak, _ = hbm_peak()
-    cfgs = set(args.configs.split(","))
+    known = {
+        "b0_1e6": ("B0 -> J/psi K pi, 10^6 events", [3.0969, K, PI], 5.27934, 10**6),
+        "b0_2e26": ("B0 -> J/psi K pi, 2^26 events", [3.0969, K, PI], 5.27934, 1 << 26),
+        "pions10_2e26": ("10 pions from M=5.0, 2^26 events", [PI] * 10, 5.0, 1 << 26),
+    }
     cases = []
-    if "1" in cfgs:
-        cases.append(("config 1: B0 -> J/psi K pi, 10^6 events", [3.0969, K, PI], 5.27934, 10**6,
-                      ("fp64", "fp32_fix"), True))
-    if "3" in cfgs:
-        cases.append(("config 3: B0 -> J/psi K pi, 2^26 events", [3.0969, K, PI], 5.27934, 1 << 26,
-                      ("fp64", "fp32_fix"), True))
-        cases.append(("config 3: 10 pions from M=5.0, 2^26 events", [PI] * 10, 5.0, 1 << 26,
-                      ("fp64", "fp32_fix"), True))
+    for w in args.workloads.split(","):
+        if w not in known:
+            ap.error(f"unknown workload {w}; known: {', '.join(known)}")
+        cases.append((*known[w], ("fp64", "fp32_fix"), True))
     for name, m, M, n, precs, check in cases:
         print(json.dumps(run_case(api, torch, name, m, M, n, precs, args.reps, peak, check)), flush=True)
         torch.cuda.empty_cache()

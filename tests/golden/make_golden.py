@@ -26,10 +26,10 @@ PI = 0.13957
 K = 0.493677
 # (name, N, engine, seed, n, M, masses, functor(sel,i,j,a,b), mother momentum)
 GEN_CASES = [
-    ("cfg1_n3_philox", 3, 0, 0x3039, 256, 5.27934, [3.0969, K, PI], (1, 0, 1, 0.0, 0.0), (0, 0, 0)),
-    ("cfg2_n5_philox", 5, 0, 0x3039, 256, 1.86484, [K, PI, PI, PI, PI], (2, 0, 1, 0.8955, 0.0473),
+    ("b0_jpsikpi_n3_philox", 3, 0, 0x3039, 256, 5.27934, [3.0969, K, PI], (1, 0, 1, 0.0, 0.0), (0, 0, 0)),
+    ("d0_kpipipipi_n5_philox", 5, 0, 0x3039, 256, 1.86484, [K, PI, PI, PI, PI], (2, 0, 1, 0.8955, 0.0473),
      (0, 0, 0)),
-    ("cfg3_n10_philox", 10, 0, 0x3039, 128, 5.0, [PI] * 10, (2, 0, 1, 0.8955, 0.0473), (0, 0, 0)),
+    ("pions_n10_philox", 10, 0, 0x3039, 128, 5.0, [PI] * 10, (2, 0, 1, 0.8955, 0.0473), (0, 0, 0)),
     ("n2_philox", 2, 0, 7, 64, 1.0, [0.2, 0.3], (1, 0, 1, 0.0, 0.0), (0, 0, 0)),
     ("n4_squares3", 4, 1, 12345, 128, 3.0, [0.1, 0.2, 0.3, 0.4], (1, 1, 3, 0.0, 0.0), (0, 0, 0)),
     ("n7_squares3", 7, 1, 99, 96, 4.0, [PI] * 4 + [K, 0.938272, PI], (2, 2, 5, 1.0, 0.1), (0, 0, 0)),
@@ -48,8 +48,8 @@ RNG_CASES = [
 ]
 # (name, N, engine, seed, n, M, masses, functor)
 AVG_CASES = [
-    ("avg_cfg1_m2", 3, 0, 0x3039, 20000, 5.27934, [3.0969, K, PI], (1, 0, 1, 0.0, 0.0)),
-    ("avg_cfg2_bw", 5, 0, 0x3039, 20000, 1.86484, [K, PI, PI, PI, PI], (2, 0, 1, 0.8955, 0.0473)),
+    ("avg_b0_jpsikpi_m2", 3, 0, 0x3039, 20000, 5.27934, [3.0969, K, PI], (1, 0, 1, 0.0, 0.0)),
+    ("avg_d0_kpipipipi_bw", 5, 0, 0x3039, 20000, 1.86484, [K, PI, PI, PI, PI], (2, 0, 1, 0.8955, 0.0473)),
     ("avg_n10_bw", 10, 0, 0x3039, 5000, 5.0, [PI] * 10, (2, 0, 1, 0.8955, 0.0473)),
     ("avg_n4_sq_one", 4, 1, 12345, 5000, 3.0, [0.1, 0.2, 0.3, 0.4], (0, 0, 1, 0.0, 0.0)),
 ]
@@ -60,7 +60,7 @@ AVG_CASES = [
 #  phase_space_range seed, range mother momentum)
 FUNCTOR_UNWEIGHT_SEED = 0x39ABDC4529B1661C   # hydra/Decays.h:261 default
 EXTRA_CASES = [
-    ("extras_cfg1_n3_philox", 3, 0, 0x3039, 1024, 5.27934, [3.0969, K, PI], (2, 1, 2, 0.8955, 0.0473), 50.0,
+    ("extras_b0_jpsikpi_n3_philox", 3, 0, 0x3039, 1024, 5.27934, [3.0969, K, PI], (2, 1, 2, 0.8955, 0.0473), 50.0,
      (20, 25), 321, (0.1, -0.2, 0.3)),
     ("extras_n5_squares3", 5, 1, 777, 512, 1.86484, [K, PI, PI, PI, PI], (1, 0, 1, 0.0, 0.0), 0.2,
      (16, 12), 0xFFFFFFFF00000005, (0.0, 0.0, 0.0)),

@@ -45,8 +45,8 @@ def test_dropin_example_matches_reference(hps, cuda, tmp_path):
     r = subprocess.run([str(exe), "256", "20000"], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     d = json.loads(r.stdout)
-    g = load_golden("cfg1_n3_philox")
-    ga = load_golden("avg_cfg1_m2")
+    g = load_golden("b0_jpsikpi_n3_philox")
+    ga = load_golden("avg_b0_jpsikpi_m2")
     assert d["max_weight"] == g["max_weight"] and d["ecm"] == g["ecm"] and d["seed"] == 12345
     four = np.array(d["four"]).reshape(256, 3, 4).transpose(1, 0, 2)
     err = float((np.abs(four - g["four"]).max(axis=2) / g["four"][:, :, 0]).max())
@@ -70,7 +70,7 @@ def test_extras_example_matches_reference(hps, cuda, tmp_path):
     """Unweight(functor), GetEventWeightFunctor(functor), the Dalitz histogram,
     PhaseSpaceIntegrator and phase_space_range through the C++ headers, against the fixture the
     reference itself produced for the same calls."""
-    g = load_golden("extras_cfg1_n3_philox")
+    g = load_golden("extras_b0_jpsikpi_n3_philox")
     n = int(g["n"])
     exe = compile_example(hps, tmp_path / "phsp_extras", SRC_EXTRAS)
     r = subprocess.run([str(exe), str(n), repr(float(g["fmax"]))], capture_output=True, text=True, timeout=300)

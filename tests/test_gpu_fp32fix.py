@@ -19,9 +19,9 @@ TOL = 1e-6
 PI, K = 0.13957, 0.493677
 
 CASES = [
-    ("n3_cfg1", 3, 0, 5.27934, [3.0969, K, PI]),
-    ("n5_cfg2", 5, 0, 1.86484, [K, PI, PI, PI, PI]),
-    ("n10_cfg3", 10, 0, 5.0, [PI] * 10),
+    ("n3_b0_jpsikpi", 3, 0, 5.27934, [3.0969, K, PI]),
+    ("n5_d0_kpipipipi", 5, 0, 1.86484, [K, PI, PI, PI, PI]),
+    ("n10_pions", 10, 0, 5.0, [PI] * 10),
     ("n2", 2, 0, 3.0, [1.0, 0.5]),
     ("n4_sq", 4, 1, 3.0, [0.1, 0.2, 0.3, 0.4]),
     ("n7_mixed", 7, 1, 6.0, [PI, K, 0.938272, PI, PI, K, PI]),
@@ -127,7 +127,7 @@ def test_fp32fix_average_on(api, torch, oracle, name, N, engine, M, masses):
 
 
 def test_fp32fix_near_coincident_uniforms(api, torch, oracle):
-    """Events 21689203-21689204 of the N=10 config-3 channel (Philox seed 0x3039) have two sorted
+    """Events 21689203-21689204 of the ten-pion channel (M = 5.0, Philox seed 0x3039) have two sorted
     uniforms only 1.4e-11 apart, so one stage sits 5e-11 GeV above threshold.  The reference's
     uniforms are double(word) / 2^64; the gap must be taken between those rounded values (the exact
     word difference differs from it by 4e-6 relative here).  The FP64 reference itself loses about

@@ -243,7 +243,7 @@ def test_event_weights_and_unweight_flags_bit_exact(api, torch, name):
 
 
 def test_decays_unweight_stable_partition(api, torch):
-    g = load_golden("cfg1_n3_philox")
+    g = load_golden("b0_jpsikpi_n3_philox")
     ps = api.PhaseSpace(float(g["M"]), list(g["masses"]), engine="philox")
     ps.SetSeed(int(g["seed"]))
     ev = ps.Generate(api.Vector4R(float(g["M"])), int(g["n"]))
@@ -323,8 +323,8 @@ def test_average_on_edges(api, torch, oracle, n):
 
 
 def test_phase_space_class_mirrors_reference(api, torch):
-    """hydra::PhaseSpace-shaped API: config-1 event 0 and AverageOn through the class."""
-    g = load_golden("cfg1_n3_philox")
+    """hydra::PhaseSpace-shaped API: B0 -> J/psi K pi event 0 and AverageOn through the class."""
+    g = load_golden("b0_jpsikpi_n3_philox")
     ps = api.PhaseSpace(5.27934, [3.0969, K, PI], engine="philox")
     ps.SetSeed(0x3039)
     assert ps.GetMaxWeight() == g["max_weight"]
@@ -333,7 +333,7 @@ def test_phase_space_class_mirrors_reference(api, torch):
     res = ps.Evaluate(api.Vector4R(5.27934), 16, api.functor_mass2(0, 1))
     assert np.array_equal(res[0].cpu().numpy(), g["w_gen"][:16])
     mean, err = ps.AverageOn(api.Vector4R(5.27934), api.functor_mass2(0, 1), 20000)
-    ga = load_golden("avg_cfg1_m2")
+    ga = load_golden("avg_b0_jpsikpi_m2")
     assert abs(mean - ga["mean"]) <= TOL_AVG * ga["mean"]
 
 

@@ -21,9 +21,9 @@ pytestmark = pytest.mark.gpu
 PI, K = 0.13957, 0.493677
 
 CASES = [
-    ("n3_cfg1", 3, "philox", 5.27934, [3.0969, K, PI], None, 0),
-    ("n5_cfg2", 5, "philox", 1.86484, [K, PI, PI, PI, PI], None, 0),
-    ("n10_cfg3", 10, "philox", 5.0, [PI] * 10, None, 1 << 20),
+    ("n3_b0_jpsikpi", 3, "philox", 5.27934, [3.0969, K, PI], None, 0),
+    ("n5_d0_kpipipipi", 5, "philox", 1.86484, [K, PI, PI, PI, PI], None, 0),
+    ("n10_pions", 10, "philox", 5.0, [PI] * 10, None, 1 << 20),
     ("n2", 2, "philox", 3.0, [1.0, 0.5], None, 7),
     ("n4_sq", 4, "squares3", 3.0, [0.1, 0.2, 0.3, 0.4], None, 0),
     ("n7_sq_moving", 7, "squares3", 6.0, [PI, K, 0.938272, PI, PI, K, PI], [6.5, 1.0, -2.0, 1.5], 99),

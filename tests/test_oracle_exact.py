@@ -2,8 +2,8 @@
 
 The reference draws its uniforms as double(word) / 2^64 and then works in IEEE double.  On a
 stage near threshold, a - b - c cancels: the FP64 weight of such an event is off by far more than
-1e-15.  These tests measure that on ordinary events and on events 21689203-21689204 of the N=10
-config-3 channel (Philox seed 0x3039), whose stage gap is 5e-11 GeV, so that the FP32_FIX
+1e-15.  These tests measure that on ordinary events and on events 21689203-21689204 of the
+ten-pion channel (M = 5.0, Philox seed 0x3039), whose stage gap is 5e-11 GeV, so that the FP32_FIX
 comparisons against the FP64 oracle can be read correctly.  CPU only; needs mpmath.
 """
 from __future__ import annotations

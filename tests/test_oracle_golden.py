@@ -90,7 +90,7 @@ def test_average_on_sequential_fold_bit_exact(oracle, name):
 
 
 def test_generate_threads_identical(oracle):
-    g = load_golden("cfg2_n5_philox")
+    g = load_golden("d0_kpipipipi_n5_philox")
     ch = _channel(oracle, g)
     a = oracle.generate(ch, 0, 3000, nthreads=1)
     b = oracle.generate(ch, 0, 3000, nthreads=0)
