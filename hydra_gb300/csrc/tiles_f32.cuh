@@ -44,14 +44,14 @@ __device__ __forceinline__ void store_event_f32(const float (&p)[N][4], const f3
 
 // Events [cb, cb + NT) of the call (event index first + e); all NT threads call together, with
 // the word-buffer parity alternating between consecutive calls (cta_event_words).
-template <int N, int ENGINE>
+template <int N, int ENGINE, int NT = kTileThreads>
 __device__ __forceinline__ void store_chunk_f32(const DevChannel& chd, const DevChannelF& ch, const Cols& cols,
                                                 double* __restrict__ weights, uint8_t* __restrict__ flags,
                                                 uint64_t ukey, uint64_t first, uint64_t n, uint64_t cb,
                                                 bool vec32, void* smem, int parity)
 {
     uint64_t w[3 * N - 4];
-    cta_event_words<N, ENGINE, kTileThreads>(chd.key, first + cb, smem, w, parity);
+    cta_event_words<N, ENGINE, NT>(chd.key, first + cb, smem, w, parity);
     const uint64_t e = cb + threadIdx.x;
     if (e < n) {
         float p[N][4];
