@@ -48,6 +48,11 @@ constexpr int kGenThreads = kTileThreads;
 // events: 9.54 ms against 10.9 ms).
 __host__ __device__ constexpr int gen_threads(int N) { return N <= 6 ? 128 : kGenThreads; }
 
+// Grid cap of the store kernel (CTAs loop over chunks beyond it).  At 2^24 events, N = 5: 152 x 128
+// CTAs 0.618 ms, x 64 0.621, x 256 0.622, x 512 0.628, one CTA per chunk 0.640, one resident wave
+// (152 x 10) 0.667.
+constexpr unsigned kGenMaxCtas = 152u * 128u;
+
 template <int N, int ENGINE>
 __global__ void __launch_bounds__(gen_threads(N))
 k_generate_f32fix(DevChannel chd, DevChannelF ch, Cols cols, double* __restrict__ weights,
@@ -136,7 +141,7 @@ hps_status hps_generate(const hps_channel* channel, uint64_t first_evt, uint64_t
         DevChannelF chf;
         to_device_channel_f(channel, &chf);
 #define HPS_BODY(NN, EE)                                                                         \
-        k_generate_f32fix<NN, EE><<<grid_for(n, gen_threads(NN), 152u * 64u), gen_threads(NN), 0, as_stream(stream)>>>(ch, chf, cc, weights, flags, ukey, \
+        k_generate_f32fix<NN, EE><<<grid_for(n, gen_threads(NN), kGenMaxCtas), gen_threads(NN), 0, as_stream(stream)>>>(ch, chf, cc, weights, flags, ukey, \
                                                                         first_evt, n, vec32);
         HPS_DISPATCH_N_ENGINE(N, channel->engine, HPS_BODY)
 #undef HPS_BODY
