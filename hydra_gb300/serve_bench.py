@@ -50,8 +50,8 @@ def percentiles(lat):
     return {"p50_ms": float(np.percentile(a, 50)), "p99_ms": float(np.percentile(a, 99)), "mean_ms": float(a.mean())}
 
 
-def run_batched(api, trace, budget_bytes, drain_s):
-    server = api.Server(budget_bytes=budget_bytes, slice_events=1 << 22, max_batch_items=1024,
+def run_batched(api, trace, budget_bytes, drain_s, slice_events=1 << 22):
+    server = api.Server(budget_bytes=budget_bytes, slice_events=slice_events, max_batch_items=1024,
                         max_inflight=8192)
     reqs = []
     for (t, N, m, M, n, mode, c) in trace:
@@ -153,15 +153,17 @@ def main(argv=None):
     ap.add_argument("--budget-gb", type=float, default=80.0)
     ap.add_argument("--plain", choices=["fp64", "fp32_fix", "none"], default="fp64")
     ap.add_argument("--drain", type=float, default=20.0, help="seconds after the last arrival to keep serving")
+    ap.add_argument("--slice-events", type=int, default=1 << 22, help="largest store slice per launch")
     args = ap.parse_args(argv)
     import torch
     from hydra_gb300 import api
     trace = make_trace(args.rate, args.duration, args.seed)
     total_events = sum(x[4] for x in trace)
-    batched = run_batched(api, trace, int(args.budget_gb * (1 << 30)), args.drain)
+    batched = run_batched(api, trace, int(args.budget_gb * (1 << 30)), args.drain, args.slice_events)
     line = {"workload": f"Poisson {args.rate:g} req/s for {args.duration:g} s ({len(trace)} requests, "
                         f"{total_events} events offered), 50% store / 50% AverageOn |BW|^2",
-            "offered_events_per_s": total_events / args.duration, "batched_fp32fix": batched}
+            "offered_events_per_s": total_events / args.duration, "slice_events": args.slice_events,
+            "batched_fp32fix": batched}
     if args.plain != "none":
         torch.cuda.empty_cache()
         plain = run_plain(api, torch, trace, args.plain, args.drain)
