@@ -1,9 +1,10 @@
 """One entry point on one channel, timed alone: Generate, AverageOn or Evaluate.
 
 Channels (Philox, seed 0x3039, mother at rest):
+  2    D0 -> K pi             M = 1.86484, m = (0.493677, 0.13957)
   3    B0 -> J/psi K pi       M = 5.27934, m = (3.0969, 0.493677, 0.13957)
-  5    D0 -> K pi pi pi pi    M = 1.86484, m = (0.493677, 0.13957 x 4)
-  6-8  six to eight pions    M = 3.0,     m = 0.13957 x N
+  4, 5 D0 -> K + 3 or 4 pi    M = 1.86484, m = (0.493677, 0.13957 x (N-1))
+  6-9  six to nine pions     M = 3.0,     m = 0.13957 x N
   10   ten pions             M = 5.0,     m = 0.13957 x 10
 The functor of AverageOn and Evaluate is |BW(m_01)|^2 (m0 = 0.8955, G0 = 0.0473); Evaluate
 stores the generation-time weight and the functor value (16 bytes per event), Generate the
@@ -20,11 +21,14 @@ import argparse
 import json
 
 CHANNELS = {
+    2: (1.86484, [0.493677, 0.13957]),
     3: (5.27934, [3.0969, 0.493677, 0.13957]),
+    4: (1.86484, [0.493677] + [0.13957] * 3),
     5: (1.86484, [0.493677] + [0.13957] * 4),
     6: (3.0, [0.13957] * 6),
     7: (3.0, [0.13957] * 7),
     8: (3.0, [0.13957] * 8),
+    9: (3.0, [0.13957] * 9),
     10: (5.0, [0.13957] * 10),
 }
 
