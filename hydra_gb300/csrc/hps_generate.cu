@@ -35,10 +35,10 @@ k_generate_f64(DevChannel ch, Cols cols, double* __restrict__ weights, uint8_t* 
 }
 
 // FP32_FIX store path: kinematics in float (light-cone boosts, exact-octant angles), weight
-// finished in double, four-vectors widened to double for the Decays columns.  Each CTA takes 256
-// consecutive events per CTA iteration and shares their random words (cta_event_words).  The unweight flag tests
-// prod(pdk) -- weight / max_weight, the quantity FlagDaugthers tests -- against u using the
-// generation-time weight.
+// finished in double, four-vectors widened to double for the Decays columns.  Each CTA takes
+// gen_threads(N) consecutive events per iteration and shares their random words
+// (cta_event_words).  The unweight flag tests prod(pdk) -- weight / max_weight, the quantity
+// FlagDaugthers tests -- against u using the generation-time weight.
 constexpr int kGenThreads = kTileThreads;
 
 // CTA size of the store kernel.  Smaller CTAs wait less at the per-chunk barrier of the shared
@@ -47,6 +47,13 @@ constexpr int kGenThreads = kTileThreads;
 // weight (N >= 7) 256 threads are faster (N = 7: 1.31 ms against 1.39 ms; N = 10 at 2^26
 // events: 9.54 ms against 10.9 ms).
 __host__ __device__ constexpr int gen_threads(int N) { return N <= 6 ? 128 : kGenThreads; }
+
+// Two events per thread and iteration (store_pair_f32: one word exchange for two chunks, and two
+// independent event bodies for the scheduler to interleave) pays where an event is short: at 2^24
+// events N = 2 0.174 ms against 0.186, N = 3 0.320 against 0.328, N = 4 0.463 against 0.469; at
+// N = 5 and 6 the doubled registers (76 and 91) cost more than it saves (0.671 against 0.618,
+// 0.900 against 0.797).
+__host__ __device__ constexpr bool gen_pair(int N) { return N <= 4; }
 
 // Grid cap of the store kernel (CTAs loop over chunks beyond it).  At 2^24 events, N = 5: 152 x 128
 // CTAs 0.618 ms, x 64 0.621, x 256 0.622, x 512 0.628, one CTA per chunk 0.640, one resident wave
@@ -59,11 +66,21 @@ k_generate_f32fix(DevChannel chd, DevChannelF ch, Cols cols, double* __restrict_
                   uint8_t* __restrict__ flags, uint64_t ukey, uint64_t first, uint64_t n, int vec32)
 {
     constexpr int NT = gen_threads(N);
-    __shared__ __align__(16) unsigned char smem[WordShare<N, ENGINE, NT>::BYTES2];
-    const uint64_t step = (uint64_t)gridDim.x * NT;
-    int parity = 0;
-    for (uint64_t cb = (uint64_t)blockIdx.x * NT; cb < n; cb += step, parity ^= 1)
-        store_chunk_f32<N, ENGINE, NT>(chd, ch, cols, weights, flags, ukey, first, n, cb, vec32 != 0, smem, parity);
+    if constexpr (gen_pair(N)) {
+        __shared__ __align__(16) unsigned char smem2[WordShare<N, ENGINE, 2 * NT>::BYTES2];
+        const uint64_t step = (uint64_t)gridDim.x * 2 * NT;
+        int parity = 0;
+        for (uint64_t cb = (uint64_t)blockIdx.x * 2 * NT; cb < n; cb += step, parity ^= 1)
+            store_pair_f32<N, ENGINE, NT>(chd, ch, cols, weights, flags, ukey, first, n, cb, vec32 != 0, smem2,
+                                          parity);
+    } else {
+        __shared__ __align__(16) unsigned char smem[WordShare<N, ENGINE, NT>::BYTES2];
+        const uint64_t step = (uint64_t)gridDim.x * NT;
+        int parity = 0;
+        for (uint64_t cb = (uint64_t)blockIdx.x * NT; cb < n; cb += step, parity ^= 1)
+            store_chunk_f32<N, ENGINE, NT>(chd, ch, cols, weights, flags, ukey, first, n, cb, vec32 != 0, smem,
+                                           parity);
+    }
 }
 
 constexpr int kMaxFunctors = 8;
@@ -141,7 +158,7 @@ hps_status hps_generate(const hps_channel* channel, uint64_t first_evt, uint64_t
         DevChannelF chf;
         to_device_channel_f(channel, &chf);
 #define HPS_BODY(NN, EE)                                                                         \
-        k_generate_f32fix<NN, EE><<<grid_for(n, gen_threads(NN), kGenMaxCtas), gen_threads(NN), 0, as_stream(stream)>>>(ch, chf, cc, weights, flags, ukey, \
+        k_generate_f32fix<NN, EE><<<grid_for(n, gen_threads(NN) * (gen_pair(NN) ? 2 : 1), kGenMaxCtas), gen_threads(NN), 0, as_stream(stream)>>>(ch, chf, cc, weights, flags, ukey, \
                                                                         first_evt, n, vec32);
         HPS_DISPATCH_N_ENGINE(N, channel->engine, HPS_BODY)
 #undef HPS_BODY

@@ -231,4 +231,59 @@ __device__ __forceinline__ void cta_event_words(uint64_t key, uint64_t e0, void*
     }
 }
 
+
+// Two chunks of NT events per call (thread t owns events e0 + t and e0 + NT + t): the 2NT
+// consecutive events' words with one barrier, laid out as cta_event_words lays out 2NT events.
+// smem holds two buffers of WordShare<N, ENGINE, 2 NT>::BYTES; parity as in cta_event_words.
+template <int N, int ENGINE, int NT>
+__device__ __forceinline__ void cta_event_words_pair(uint64_t key, uint64_t e0, void* smem,
+                                                     uint64_t (&wa)[3 * N - 4], uint64_t (&wb)[3 * N - 4],
+                                                     int parity)
+{
+    using S = WordShare<N, ENGINE, 2 * NT>;
+    const int t = threadIdx.x;
+    smem = static_cast<unsigned char*>(smem) + (parity & 1) * S::BYTES;
+    if constexpr (ENGINE == kPhilox) {
+        ulonglong2* slots = static_cast<ulonglong2*>(smem);
+        const uint64_t c_first = e0 + 3u * N + 1u;
+        if (e0 <= ~uint64_t(0) - (3u * N + S::SLOTS)) {
+            uint64_t o0, o1;
+            philox2x64_7(c_first + t, 0, key, o0, o1);
+            slots[t] = make_ulonglong2(o0, o1);
+            philox2x64_7(c_first + NT + t, 0, key, o0, o1);
+            slots[NT + t] = make_ulonglong2(o0, o1);
+            if (t < S::B - 1) {
+                philox2x64_7(c_first + 2 * NT + t, 0, key, o0, o1);
+                slots[2 * NT + t] = make_ulonglong2(o0, o1);
+            }
+            __syncthreads();
+#pragma unroll
+            for (int b = 0; b < S::B; ++b) {
+                const ulonglong2 va = slots[t + b], vb = slots[NT + t + b];
+                wa[2 * b] = va.x;
+                wb[2 * b] = vb.x;
+                if (2 * b + 1 < S::NW) {
+                    wa[2 * b + 1] = va.y;
+                    wb[2 * b + 1] = vb.y;
+                }
+            }
+        } else {
+            event_words<N, kPhilox>(key, e0 + t, wa);
+            event_words<N, kPhilox>(key, e0 + NT + t, wb);
+        }
+    } else {
+        uint64_t* slots = static_cast<uint64_t*>(smem);
+        const uint64_t c_first = e0 + 3u * N;
+        slots[t] = squares3_word(key, c_first + t);
+        slots[NT + t] = squares3_word(key, c_first + NT + t);
+        if (t < S::B - 1) slots[2 * NT + t] = squares3_word(key, c_first + 2 * NT + t);
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < S::NW; ++k) {
+            wa[k] = slots[t + k];
+            wb[k] = slots[NT + t + k];
+        }
+    }
+}
+
 }  // namespace hps

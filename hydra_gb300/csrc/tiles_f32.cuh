@@ -60,6 +60,24 @@ __device__ __forceinline__ void store_chunk_f32(const DevChannel& chd, const Dev
     }
 }
 
+// Events [cb, cb + 2 NT): thread t computes events cb + t and cb + NT + t from one word exchange
+// (both are computed whatever n is; only events below n are stored).
+template <int N, int ENGINE, int NT>
+__device__ __forceinline__ void store_pair_f32(const DevChannel& chd, const DevChannelF& ch, const Cols& cols,
+                                               double* __restrict__ weights, uint8_t* __restrict__ flags,
+                                               uint64_t ukey, uint64_t first, uint64_t n, uint64_t cb,
+                                               bool vec32, void* smem, int parity)
+{
+    uint64_t wa[3 * N - 4], wb[3 * N - 4];
+    cta_event_words_pair<N, ENGINE, NT>(chd.key, first + cb, smem, wa, wb, parity);
+    const uint64_t ea = cb + threadIdx.x, eb = ea + NT;
+    float pa[N][4], pb[N][4];
+    const f32::EventWeight wta = f32::event_from_words<N, ENGINE>(chd, ch, wa, pa);
+    const f32::EventWeight wtb = f32::event_from_words<N, ENGINE>(chd, ch, wb, pb);
+    if (ea < n) store_event_f32<N>(pa, wta, cols, weights, flags, ukey, first, ea, vec32);
+    if (eb < n) store_event_f32<N>(pb, wtb, cols, weights, flags, ukey, first, eb, vec32);
+}
+
 __device__ __forceinline__ void ff_add(float& sh, float& sl, float xh, float xl)
 {
     const float s = sh + xh;
