@@ -35,10 +35,10 @@ k_generate_f64(DevChannel ch, Cols cols, double* __restrict__ weights, uint8_t* 
 }
 
 // FP32_FIX store path: kinematics in float (light-cone boosts, exact-octant angles), weight
-// finished in double, four-vectors widened to double for the Decays columns.  Each CTA takes
-// gen_threads(N) consecutive events per iteration and shares their random words
-// (cta_event_words).  The unweight flag tests prod(pdk) -- weight / max_weight, the quantity
-// FlagDaugthers tests -- against u using the generation-time weight.
+// finished in double, four-vectors widened to double for the Decays columns.  Each CTA takes two
+// chunks of gen_threads(N) consecutive events per iteration and shares their random words
+// (cta_event_words_pair, cta_words_pair_fill).  The unweight flag tests prod(pdk) -- weight /
+// max_weight, the quantity FlagDaugthers tests -- against u using the generation-time weight.
 constexpr int kGenThreads = kTileThreads;
 
 // CTA size of the store kernel.  Smaller CTAs wait less at the per-chunk barrier of the shared
@@ -54,6 +54,13 @@ __host__ __device__ constexpr int gen_threads(int N) { return N <= 6 ? 128 : kGe
 // N = 5 and 6 the doubled registers (76 and 91) cost more than it saves (0.671 against 0.618,
 // 0.900 against 0.797).
 __host__ __device__ constexpr bool gen_pair(int N) { return N <= 4; }
+// From N = 5 on, the two events of an iteration are computed one after the other from the same
+// word exchange (store_pair_seq_f32: the registers of one event, one barrier per two chunks):
+// N = 5 0.613 ms against 0.618, N = 7 1.284 against 1.298, N = 10 2.254 against 2.326; N = 8
+// 1.570 against 1.562.
+
+// Every form takes two chunks of gen_threads(N) events per CTA iteration.
+__host__ __device__ constexpr int gen_events_per_iteration(int N) { return 2 * gen_threads(N); }
 
 // Grid cap of the store kernel (CTAs loop over chunks beyond it).  At 2^24 events, N = 5: 152 x 128
 // CTAs 0.618 ms, x 64 0.621, x 256 0.622, x 512 0.628, one CTA per chunk 0.640, one resident wave
@@ -66,20 +73,16 @@ k_generate_f32fix(DevChannel chd, DevChannelF ch, Cols cols, double* __restrict_
                   uint8_t* __restrict__ flags, uint64_t ukey, uint64_t first, uint64_t n, int vec32)
 {
     constexpr int NT = gen_threads(N);
-    if constexpr (gen_pair(N)) {
-        __shared__ __align__(16) unsigned char smem2[WordShare<N, ENGINE, 2 * NT>::BYTES2];
-        const uint64_t step = (uint64_t)gridDim.x * 2 * NT;
-        int parity = 0;
-        for (uint64_t cb = (uint64_t)blockIdx.x * 2 * NT; cb < n; cb += step, parity ^= 1)
-            store_pair_f32<N, ENGINE, NT>(chd, ch, cols, weights, flags, ukey, first, n, cb, vec32 != 0, smem2,
+    __shared__ __align__(16) unsigned char smem[WordShare<N, ENGINE, 2 * NT>::BYTES2];
+    const uint64_t step = (uint64_t)gridDim.x * gen_events_per_iteration(N);
+    int parity = 0;
+    for (uint64_t cb = (uint64_t)blockIdx.x * gen_events_per_iteration(N); cb < n; cb += step, parity ^= 1) {
+        if constexpr (gen_pair(N))
+            store_pair_f32<N, ENGINE, NT>(chd, ch, cols, weights, flags, ukey, first, n, cb, vec32 != 0, smem,
                                           parity);
-    } else {
-        __shared__ __align__(16) unsigned char smem[WordShare<N, ENGINE, NT>::BYTES2];
-        const uint64_t step = (uint64_t)gridDim.x * NT;
-        int parity = 0;
-        for (uint64_t cb = (uint64_t)blockIdx.x * NT; cb < n; cb += step, parity ^= 1)
-            store_chunk_f32<N, ENGINE, NT>(chd, ch, cols, weights, flags, ukey, first, n, cb, vec32 != 0, smem,
-                                           parity);
+        else
+            store_pair_seq_f32<N, ENGINE, NT>(chd, ch, cols, weights, flags, ukey, first, n, cb, vec32 != 0, smem,
+                                              parity);
     }
 }
 
@@ -158,7 +161,7 @@ hps_status hps_generate(const hps_channel* channel, uint64_t first_evt, uint64_t
         DevChannelF chf;
         to_device_channel_f(channel, &chf);
 #define HPS_BODY(NN, EE)                                                                         \
-        k_generate_f32fix<NN, EE><<<grid_for(n, gen_threads(NN) * (gen_pair(NN) ? 2 : 1), kGenMaxCtas), gen_threads(NN), 0, as_stream(stream)>>>(ch, chf, cc, weights, flags, ukey, \
+        k_generate_f32fix<NN, EE><<<grid_for(n, gen_events_per_iteration(NN), kGenMaxCtas), gen_threads(NN), 0, as_stream(stream)>>>(ch, chf, cc, weights, flags, ukey, \
                                                                         first_evt, n, vec32);
         HPS_DISPATCH_N_ENGINE(N, channel->engine, HPS_BODY)
 #undef HPS_BODY

@@ -286,4 +286,60 @@ __device__ __forceinline__ void cta_event_words_pair(uint64_t key, uint64_t e0, 
     }
 }
 
+
+// The fill half of cta_event_words_pair: the 2NT events' words into the parity buffer and one
+// barrier.  Returns false (and writes nothing) near the end of the counter range, where each
+// thread computes its own words.
+template <int N, int ENGINE, int NT>
+__device__ __forceinline__ bool cta_words_pair_fill(uint64_t key, uint64_t e0, void* smem, int parity)
+{
+    using S = WordShare<N, ENGINE, 2 * NT>;
+    const int t = threadIdx.x;
+    smem = static_cast<unsigned char*>(smem) + (parity & 1) * S::BYTES;
+    if constexpr (ENGINE == kPhilox) {
+        if (!(e0 <= ~uint64_t(0) - (3u * N + S::SLOTS))) return false;
+        ulonglong2* slots = static_cast<ulonglong2*>(smem);
+        const uint64_t c_first = e0 + 3u * N + 1u;
+        uint64_t o0, o1;
+        philox2x64_7(c_first + t, 0, key, o0, o1);
+        slots[t] = make_ulonglong2(o0, o1);
+        philox2x64_7(c_first + NT + t, 0, key, o0, o1);
+        slots[NT + t] = make_ulonglong2(o0, o1);
+        if (t < S::B - 1) {
+            philox2x64_7(c_first + 2 * NT + t, 0, key, o0, o1);
+            slots[2 * NT + t] = make_ulonglong2(o0, o1);
+        }
+    } else {
+        uint64_t* slots = static_cast<uint64_t*>(smem);
+        const uint64_t c_first = e0 + 3u * N;
+        slots[t] = squares3_word(key, c_first + t);
+        slots[NT + t] = squares3_word(key, c_first + NT + t);
+        if (t < S::B - 1) slots[2 * NT + t] = squares3_word(key, c_first + 2 * NT + t);
+    }
+    __syncthreads();
+    return true;
+}
+
+// The read half: the words of event e0 + h NT + t (h = 0 or 1) from the filled buffer.
+template <int N, int ENGINE, int NT>
+__device__ __forceinline__ void cta_words_pair_read(const void* smem, int parity, int h, uint64_t (&w)[3 * N - 4])
+{
+    using S = WordShare<N, ENGINE, 2 * NT>;
+    const int t = threadIdx.x + h * NT;
+    smem = static_cast<const unsigned char*>(smem) + (parity & 1) * S::BYTES;
+    if constexpr (ENGINE == kPhilox) {
+        const ulonglong2* slots = static_cast<const ulonglong2*>(smem);
+#pragma unroll
+        for (int b = 0; b < S::B; ++b) {
+            const ulonglong2 v = slots[t + b];
+            w[2 * b] = v.x;
+            if (2 * b + 1 < S::NW) w[2 * b + 1] = v.y;
+        }
+    } else {
+        const uint64_t* slots = static_cast<const uint64_t*>(smem);
+#pragma unroll
+        for (int k = 0; k < S::NW; ++k) w[k] = slots[t + k];
+    }
+}
+
 }  // namespace hps

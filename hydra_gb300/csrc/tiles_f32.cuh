@@ -78,6 +78,29 @@ __device__ __forceinline__ void store_pair_f32(const DevChannel& chd, const DevC
     if (eb < n) store_event_f32<N>(pb, wtb, cols, weights, flags, ukey, first, eb, vec32);
 }
 
+// Events [cb, cb + 2 NT) with one word exchange, computed one after the other (thread t: event
+// cb + t, then cb + NT + t), so the registers are those of one event.
+template <int N, int ENGINE, int NT>
+__device__ __forceinline__ void store_pair_seq_f32(const DevChannel& chd, const DevChannelF& ch, const Cols& cols,
+                                                   double* __restrict__ weights, uint8_t* __restrict__ flags,
+                                                   uint64_t ukey, uint64_t first, uint64_t n, uint64_t cb,
+                                                   bool vec32, void* smem, int parity)
+{
+    const bool shared = cta_words_pair_fill<N, ENGINE, NT>(chd.key, first + cb, smem, parity);
+#pragma unroll 1
+    for (int h = 0; h < 2; ++h) {
+        const uint64_t e = cb + (uint64_t)h * NT + threadIdx.x;
+        uint64_t w[3 * N - 4];
+        if (shared) cta_words_pair_read<N, ENGINE, NT>(smem, parity, h, w);
+        else event_words<N, ENGINE>(chd.key, first + e, w);
+        if (e < n) {
+            float p[N][4];
+            const f32::EventWeight ew = f32::event_from_words<N, ENGINE>(chd, ch, w, p);
+            store_event_f32<N>(p, ew, cols, weights, flags, ukey, first, e, vec32);
+        }
+    }
+}
+
 __device__ __forceinline__ void ff_add(float& sh, float& sl, float xh, float xl)
 {
     const float s = sh + xh;
