@@ -17,6 +17,11 @@ namespace hps {
 
 constexpr int kAvgThreads = kTileThreads;
 
+// The AverageOn tiles exchange the random words of two chunks at a time up to N = 6 (the same
+// sums bit for bit, half the barriers): at 2^24 events N = 5 0.574 ms against 0.577, and the
+// one-pass Generate + AverageOn 0.695 against 0.705; at N = 10 2.127 against 2.080.
+__host__ __device__ constexpr bool avg_paired(int N) { return N <= 6; }
+
 template <int N, int ENGINE>
 __global__ void __launch_bounds__(kAvgThreads)
 k_average_tiles_f64(DevChannel ch, DevFunctor fn, uint64_t first, uint64_t n, uint64_t ntiles,
@@ -81,10 +86,11 @@ __global__ void __launch_bounds__(kAvgThreads)
 k_average_tiles_f32fix(DevChannel chd, DevChannelF ch, DevFunctor fn, uint64_t first, uint64_t n,
                        uint64_t ntiles, hps_stats* __restrict__ partials, const float* __restrict__ k0)
 {
-    __shared__ __align__(16) unsigned char smem[WordShare<N, ENGINE, kAvgThreads>::BYTES2];
+    __shared__ __align__(16) unsigned char smem[PairedSmem<N, ENGINE>::BYTES];
     const float K0 = *k0;
     for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const hps_sums r = average_tile_f32<N, ENGINE>(chd, ch, fn, first, n, t, K0, smem);
+        const hps_sums r =
+            average_tile_f32<N, ENGINE, false, false, avg_paired(N)>(chd, ch, fn, first, n, t, K0, smem);
         if (threadIdx.x == 0) reinterpret_cast<hps_sums*>(partials)[t] = r;
     }
 }
@@ -95,10 +101,11 @@ k_generate_average_f32fix(DevChannel chd, DevChannelF ch, DevFunctor fn, uint64_
                           uint64_t ntiles, hps_stats* __restrict__ partials, const float* __restrict__ k0,
                           StoreOut so)
 {
-    __shared__ __align__(16) unsigned char smem[WordShare<N, ENGINE, kAvgThreads>::BYTES2];
+    __shared__ __align__(16) unsigned char smem[PairedSmem<N, ENGINE>::BYTES];
     const float K0 = *k0;
     for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const hps_sums r = average_tile_f32<N, ENGINE, true>(chd, ch, fn, first, n, t, K0, smem, &so);
+        const hps_sums r =
+            average_tile_f32<N, ENGINE, true, false, avg_paired(N)>(chd, ch, fn, first, n, t, K0, smem, &so);
         if (threadIdx.x == 0) reinterpret_cast<hps_sums*>(partials)[t] = r;
     }
 }

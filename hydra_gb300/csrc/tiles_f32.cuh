@@ -17,6 +17,11 @@ constexpr int kAvgPerThread = HPS_AVG_TILE / kTileThreads;
 static_assert(kTileThreads * kAvgPerThread == HPS_AVG_TILE, "tile shape");
 constexpr int kFinalThreads = 1024;
 
+// Shared memory of a CTA whose work units exchange the words of two chunks at a time.
+template <int N, int ENGINE> struct PairedSmem {
+    static constexpr int BYTES = WordShare<N, ENGINE, 2 * kTileThreads>::BYTES2;
+};
+
 // Where a storing work unit puts event e of the call: Decays columns, weight, unweight flag.
 struct StoreOut {
     Cols cols;
@@ -197,7 +202,7 @@ __device__ __forceinline__ float mother_functor_f32(const DevFunctor& fn, const 
     return f32::functor<N + 1>(fn, pm);
 }
 
-template <int N, int ENGINE, bool STORE = false, bool MOTHERS = false>
+template <int N, int ENGINE, bool STORE = false, bool MOTHERS = false, bool PAIRED = false>
 __device__ __forceinline__ hps_sums average_tile_f32(const DevChannel& chd, const DevChannelF& ch,
                                                      const DevFunctor& fn, uint64_t first, uint64_t n,
                                                      uint64_t t, float K0, void* smem,
@@ -207,13 +212,8 @@ __device__ __forceinline__ hps_sums average_tile_f32(const DevChannel& chd, cons
     static_assert(!(STORE && MOTHERS), "a storing tile keeps the events in the decay's rest frame");
     float swh = 0.0f, swl = 0.0f, s1h = 0.0f, s1l = 0.0f, s2h = 0.0f, s2l = 0.0f;
     const uint64_t base = t * HPS_AVG_TILE;
-    for (int k = 0; k < kAvgPerThread; ++k) {
-        const uint64_t cb = base + (uint64_t)k * kTileThreads;
-        if (cb >= n) break;                                              // CTA-uniform
-        uint64_t w[3 * N - 4];
-        cta_event_words<N, ENGINE, kTileThreads>(chd.key, first + cb, smem, w, k);
-        const uint64_t e = cb + threadIdx.x;
-        if (e < n) {
+    // one event of the tile from its words: functor, weight, and the shifted sums
+    auto add_event = [&](uint64_t e, uint64_t (&w)[3 * N - 4]) {
             float p[N][4];
             const f32::EventWeight ew = f32::event_from_words<N, ENGINE>(chd, ch, w, p);
             if constexpr (STORE)
@@ -236,6 +236,32 @@ __device__ __forceinline__ hps_sums average_tile_f32(const DevChannel& chd, cons
             ff_add(swh, swl, ew.prod_hi, ew.prod_lo);
             ff_add(s1h, s1l, h1, l1);
             ff_add(s2h, s2l, h2, l2);
+    };
+    if constexpr (PAIRED) {
+        // chunks in pairs: one word exchange for two chunks, a thread's two events in turn (the same
+        // events in the same order as one chunk at a time, so the same sums bit for bit)
+        static_assert(kAvgPerThread % 2 == 0, "chunks in pairs");
+        for (int kp = 0; kp < kAvgPerThread / 2; ++kp) {
+            const uint64_t cb = base + (uint64_t)(2 * kp) * kTileThreads;
+            if (cb >= n) break;                                          // CTA-uniform
+            const bool shared = cta_words_pair_fill<N, ENGINE, kTileThreads>(chd.key, first + cb, smem, kp);
+#pragma unroll 1
+            for (int h = 0; h < 2; ++h) {
+                const uint64_t e = cb + (uint64_t)h * kTileThreads + threadIdx.x;
+                uint64_t w[3 * N - 4];
+                if (shared) cta_words_pair_read<N, ENGINE, kTileThreads>(smem, kp, h, w);
+                else event_words<N, ENGINE>(chd.key, first + e, w);
+                if (e < n) add_event(e, w);
+            }
+        }
+    } else {
+        for (int k = 0; k < kAvgPerThread; ++k) {
+            const uint64_t cb = base + (uint64_t)k * kTileThreads;
+            if (cb >= n) break;                                          // CTA-uniform
+            uint64_t w[3 * N - 4];
+            cta_event_words<N, ENGINE, kTileThreads>(chd.key, first + cb, smem, w, k);
+            const uint64_t e = cb + threadIdx.x;
+            if (e < n) add_event(e, w);
         }
     }
     hps_sums acc;
