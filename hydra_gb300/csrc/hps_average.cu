@@ -17,10 +17,11 @@ namespace hps {
 
 constexpr int kAvgThreads = kTileThreads;
 
-// The AverageOn tiles exchange the random words of two chunks at a time up to N = 6 (the same
-// sums bit for bit, half the barriers): at 2^24 events N = 5 0.574 ms against 0.577, and the
-// one-pass Generate + AverageOn 0.695 against 0.705; at N = 10 2.127 against 2.080.
-__host__ __device__ constexpr bool avg_paired(int N) { return N <= 6; }
+// The AverageOn tiles exchange the random words of two chunks at a time for N = 3..5 (the same
+// sums bit for bit, half the barriers): at 2^24 events N = 3 0.306 ms against 0.309, N = 5 0.575
+// against 0.577, and the one-pass Generate + AverageOn at N = 5 0.694 against 0.705; at N = 2
+// 0.191 against 0.188, N = 6 0.760 against 0.735, N = 10 2.127 against 2.080.
+__host__ __device__ constexpr bool avg_paired(int N) { return N >= 3 && N <= 5; }
 
 template <int N, int ENGINE>
 __global__ void __launch_bounds__(kAvgThreads)
