@@ -53,14 +53,21 @@ __host__ __device__ constexpr int gen_threads(int N) { return N <= 6 ? 128 : kGe
 // events N = 2 0.174 ms against 0.186, N = 3 0.320 against 0.328, N = 4 0.463 against 0.469; at
 // N = 5 and 6 the doubled registers (76 and 91) cost more than it saves (0.671 against 0.618,
 // 0.900 against 0.797).
-__host__ __device__ constexpr bool gen_pair(int N) { return N <= 4; }
 // From N = 5 on, the two events of an iteration are computed one after the other from the same
 // word exchange (store_pair_seq_f32: the registers of one event, one barrier per two chunks):
-// N = 5 0.613 ms against 0.618, N = 7 1.284 against 1.298, N = 10 2.254 against 2.326; N = 8
-// 1.570 against 1.562.
+// N = 5 0.613 ms against 0.618, N = 7 1.284 against 1.298, N = 10 2.254 against 2.326.  N = 8
+// and 9 keep one exchange per chunk (store_chunk_f32; N = 8: 1.562 against 1.570).
+enum : int { kGenChunk = 0, kGenPair = 1, kGenPairSeq = 2 };
+__host__ __device__ constexpr int gen_form(int N)
+{
+    return N <= 4 ? kGenPair : (N == 8 || N == 9) ? kGenChunk : kGenPairSeq;
+}
 
-// Every form takes two chunks of gen_threads(N) events per CTA iteration.
-__host__ __device__ constexpr int gen_events_per_iteration(int N) { return 2 * gen_threads(N); }
+// Events a CTA takes per iteration: two chunks of gen_threads(N) events, or one.
+__host__ __device__ constexpr int gen_events_per_iteration(int N)
+{
+    return gen_form(N) == kGenChunk ? gen_threads(N) : 2 * gen_threads(N);
+}
 
 // Grid cap of the store kernel (CTAs loop over chunks beyond it).  At 2^24 events, N = 5: 152 x 128
 // CTAs 0.618 ms, x 64 0.621, x 256 0.622, x 512 0.628, one CTA per chunk 0.640, one resident wave
@@ -77,12 +84,15 @@ k_generate_f32fix(DevChannel chd, DevChannelF ch, Cols cols, double* __restrict_
     const uint64_t step = (uint64_t)gridDim.x * gen_events_per_iteration(N);
     int parity = 0;
     for (uint64_t cb = (uint64_t)blockIdx.x * gen_events_per_iteration(N); cb < n; cb += step, parity ^= 1) {
-        if constexpr (gen_pair(N))
+        if constexpr (gen_form(N) == kGenPair)
             store_pair_f32<N, ENGINE, NT>(chd, ch, cols, weights, flags, ukey, first, n, cb, vec32 != 0, smem,
                                           parity);
-        else
+        else if constexpr (gen_form(N) == kGenPairSeq)
             store_pair_seq_f32<N, ENGINE, NT>(chd, ch, cols, weights, flags, ukey, first, n, cb, vec32 != 0, smem,
                                               parity);
+        else
+            store_chunk_f32<N, ENGINE, NT>(chd, ch, cols, weights, flags, ukey, first, n, cb, vec32 != 0, smem,
+                                           parity);
     }
 }
 
