@@ -13,6 +13,17 @@ exceed the 129 MB L2, so no flush is needed between steps.
 
 --impl reference times the reference algorithm on the host cores (the oracle port of
 Hydra's cpp/omp path, all threads) on a bounded sample of the same workload.
+
+After the contract's timed loop, `parts` adds the other workloads the metric names, each timed
+once on the same GPU (skip with --no-parts):
+  * the same N=5 workload at FP64 (the reference's arithmetic): Generate and AverageOn ms;
+  * 256 channels of N in 2..10 (seeded mix, ~37 M events) as one batched graph launch: events/s,
+    fraction of the HBM copy peak, max relative error against the FP64 form of the same events;
+  * a seeded Poisson serving trace (2000 requests/s, 50% store / 50% AverageOn |BW|^2): p50/p99
+    latency and served events/s of the continuous-batching server, the same trace through the
+    plain FP64 one-launch-per-request form, and their throughput ratio;
+  * a capacity sweep: the arrival rate raised until the server no longer keeps up, with the
+    saturated events/s and its p99.
 """
 from __future__ import annotations
 
@@ -337,6 +348,18 @@ def run_gpu(args):
     precision_report = None
     if rank == 0 and not args.no_check:
         precision_report = check_against_oracle(api, torch, ch, fn, first, four, w, fl, stats, args)
+        if not args.no_parts:
+            precision_report["full_size_fp32_fix_vs_fp64"] = precision_part(api, torch)
+
+    extra = {}
+    if rank == 0 and not args.no_parts:
+        peak_gbs = measured_peak_hbm()[0]
+        extra["fp64_same_workload"] = fp64_part(api, torch, ch, fn, four, w, fl, stats, ws, first, n, stream)
+        del four, w, fl, ws
+        torch.cuda.empty_cache()
+        extra["batched_256_channels"] = batch_part(api, torch, peak_gbs)
+        extra["serving"] = serving_part(api, torch)
+        extra["serving_capacity"] = capacity_part(api, torch)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -357,7 +380,7 @@ def run_gpu(args):
                       "fused_generate_average_ms": fused_ms,
                       "fused_events_per_s": world * n / (fused_ms / 1e3),
                       "fused_note": "hps_generate_average: the same Decays, weights, flags and AverageOn "
-                                    "result in one pass (bit-identical), not part of value"},
+                                    "result in one pass (bit-identical), not part of value", **extra},
             "max_rel_err": precision_report,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": (4 if args.precision == "fp32_fix" else 3) * args.steps, "clocks": csum,
@@ -367,6 +390,135 @@ def run_gpu(args):
         import torch.distributed as dist
         dist.destroy_process_group()
     return 0
+
+
+def timed_ms(torch, fn, reps, stream=None):
+    """Median of `reps` CUDA-event timings of fn() after one untimed call."""
+    fn()
+    torch.cuda.synchronize()
+    out = []
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        out.append(a.elapsed_time(b))
+    return statistics.median(out)
+
+
+def fp64_part(api, torch, ch, fn, four, w, fl, stats, ws, first, n, stream):
+    """The bench workload at FP64 (the reference's arithmetic), Generate and AverageOn timed alone."""
+    g = timed_ms(torch, lambda: api.generate(ch, first, four, w, fl, UNWEIGHT_SEED, "fp64", stream), 3, stream)
+    a = timed_ms(torch, lambda: api.average_on(ch, first, n, fn, stats, ws, "fp64", stream), 3, stream)
+    return {"generate_ms": g, "average_on_ms": a, "generate_events_per_s": n / (g / 1e3),
+            "average_on_events_per_s": n / (a / 1e3), "pipeline_events_per_s": n / ((g + a) / 1e3)}
+
+
+def precision_part(api, torch, total=1 << 26, chunk=1 << 22):
+    """The precision workloads at full size: every one of 2^26 events of ten pions from M = 5.0 GeV
+    and of B0 -> J/psi K pi, FP32_FIX against the FP64 form of the same events (which follows the
+    reference's arithmetic operation for operation)."""
+    out = {}
+    for name, M, masses in (("ten_pions_M5_2e26", 5.0, [0.13957] * 10),
+                            ("b0_jpsi_k_pi_2e26", 5.27934, [3.0969, 0.493677, 0.13957])):
+        N = len(masses)
+        ch = api.make_channel(masses, M, SEED, "philox")
+        a = torch.empty((N, chunk, 4), dtype=torch.float64, device="cuda")
+        b = torch.empty_like(a)
+        wa = torch.empty(chunk, dtype=torch.float64, device="cuda")
+        wb = torch.empty_like(wa)
+        e4 = ew = 0.0
+        for first in range(0, total, chunk):
+            api.generate(ch, first, a, wa, None, precision="fp32_fix")
+            api.generate(ch, first, b, wb, None, precision="fp64")
+            e4 = max(e4, float(((a - b).abs().amax(dim=2) / b[:, :, 0]).max()))
+            ew = max(ew, float(((wa - wb).abs() / wb).max()))
+        out[name] = {"four_vectors": e4, "weights": ew, "events_checked": total}
+        del a, b, wa, wb
+        torch.cuda.empty_cache()
+    return out
+
+
+def batch_part(api, torch, peak, n_channels=256, check_channels=32):
+    """256 seeded channels (N uniform in 2..10, masses from the menu, events log-uniform 1e3..1e6),
+    store path, one graph launch of the batched FP32_FIX kernels after the project's autotuner."""
+    from hydra_gb300 import batch_bench as BB
+    chans = BB.make_channels(n_channels)
+    total = sum(c[3] for c in chans)
+    nbytes = sum(c[3] * (32 * c[0] + 8) for c in chans)
+    outs, items, hch = [], [], []
+    for N, m, M, n, seed in chans:
+        ch = api.make_channel(m, M, seed, "philox")
+        four = torch.empty((N, n, 4), dtype=torch.float64, device="cuda")
+        w = torch.empty(n, dtype=torch.float64, device="cuda")
+        outs.append((four, w))
+        hch.append(ch)
+        items.append(api.store_item(ch, 0, four, w))
+    plan = api.BatchPlan(len(items), 1)
+    plan.set_items(items)
+    t0 = time.perf_counter()
+    tuning = plan.autotune(None)
+    tune_s = time.perf_counter() - t0
+    ms = timed_ms(torch, plan.launch, 5)
+    plan.launch()
+    torch.cuda.synchronize()
+    # every event of the first `check_channels` channels against the FP64 form of the same events
+    e4 = ew = 0.0
+    for ch, (four, w) in list(zip(hch, outs))[:check_channels]:
+        f64, w64 = torch.empty_like(four), torch.empty_like(w)
+        api.generate(ch, 0, f64, w64, None, precision="fp64")
+        e4 = max(e4, float(((four - f64).abs().amax(dim=2) / f64[:, :, 0]).max()))
+        ew = max(ew, float(((w - w64).abs() / w64).max()))
+    checked = sum(c[3] for c in chans[:check_channels])
+    plan.close()
+    del outs, items
+    torch.cuda.empty_cache()
+    gbs = nbytes / (ms / 1e3) / 1e9
+    return {"workload": f"{n_channels} channels, N in 2..10, {total} events, store path (32N+8 B/event)",
+            "events": total, "ms": ms, "events_per_s": total / (ms / 1e3), "gbs": gbs, "hbm_frac": gbs / peak,
+            "tuning": {"ctas_per_sm": tuning[0], "store_tile_events": tuning[1],
+                       "kernel_form": ["per_N", "one_kernel"][tuning[2]], "autotune_s": tune_s},
+            "max_rel_err": {"four_vectors": e4, "weights": ew, "events_checked": checked,
+                            "against": "FP64 form of the same events"}}
+
+
+def serving_part(api, torch, rate=2000.0, duration=3.0, budget_gb=80.0, drain_plain=4.0):
+    """A seeded Poisson trace through the continuous-batching server, then the same trace through
+    the plain FP64 one-launch-per-request form (its unfinished requests are reported as backlog)."""
+    from hydra_gb300 import serve_bench as SB
+    trace = SB.make_trace(rate, duration, 12345)
+    offered = sum(x[4] for x in trace)
+    served = SB.run_batched(api, trace, int(budget_gb * (1 << 30)), 30.0)
+    torch.cuda.empty_cache()
+    plain = SB.run_plain(api, torch, trace, "fp64", drain_plain)
+    torch.cuda.empty_cache()
+    ratio = served["events_per_s"] / plain["events_per_s"] if plain["events_per_s"] else None
+    return {"workload": f"Poisson {rate:g} req/s for {duration:g} s, seed 12345 ({len(trace)} requests, "
+                        f"{offered} events), 50% store / 50% AverageOn |BW|^2, {budget_gb:g} GB budget",
+            "offered_events_per_s": offered / duration,
+            "served_fp32fix_batched": served, "plain_fp64_per_request": plain,
+            "throughput_ratio_vs_plain_fp64": ratio}
+
+
+def capacity_part(api, torch, rates=(2000.0, 8000.0, 32000.0), duration=1.0, budget_gb=80.0):
+    """Arrival rate raised until the served throughput falls behind the offered load: the
+    saturated events/s of the server and the p99 latency at that load."""
+    from hydra_gb300 import serve_bench as SB
+    points = []
+    for i, rate in enumerate(rates):
+        trace = SB.make_trace(rate, duration, 777 + i)
+        offered = sum(x[4] for x in trace) / duration
+        r = SB.run_batched(api, trace, int(budget_gb * (1 << 30)), 60.0)
+        torch.cuda.empty_cache()
+        points.append({"rate_req_per_s": rate, "requests": len(trace), "offered_events_per_s": offered,
+                       "served_events_per_s": r["events_per_s"], "p50_ms": r["p50_ms"], "p99_ms": r["p99_ms"],
+                       "completed": r["completed"]})
+        if r["events_per_s"] < 0.8 * offered:
+            break
+    sat = max(points, key=lambda p: p["served_events_per_s"])
+    return {"points": points, "saturated_events_per_s": sat["served_events_per_s"], "p99_ms_at_saturation":
+            sat["p99_ms"], "saturated": points[-1]["served_events_per_s"] < 0.8 * points[-1]["offered_events_per_s"]}
 
 
 def check_against_oracle(api, torch, ch, fn, first, four, w, fl, stats, args, sample=1 << 18):
@@ -409,6 +561,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-check", action="store_true")
+    ap.add_argument("--no-parts", action="store_true", help="skip the FP64, batch and serving parts")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -1,6 +1,7 @@
 // common.h -- host-side helpers shared by the C-ABI translation units of libhps.so.
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
@@ -15,6 +16,22 @@ namespace hps {
 // Per-thread message behind hps_last_error().
 hps_status set_error(hps_status st, const char* fmt, ...);
 void clear_error();
+
+// Opening of every C-ABI call: clears the calling thread's error message and keeps an NVTX range
+// named after the call open for its duration, so a profiler's timeline (Nsight Systems, Nsight
+// Compute's NVTX filter) shows each library call around the kernels it launched.  Without a tool
+// attached an NVTX push/pop is a test of a null function pointer.
+struct EntryScope {
+    explicit EntryScope(const char* name)
+    {
+        clear_error();
+        nvtxRangePushA(name);
+    }
+    ~EntryScope() { nvtxRangePop(); }
+    EntryScope(const EntryScope&) = delete;
+    EntryScope& operator=(const EntryScope&) = delete;
+};
+#define HPS_ENTRY() const ::hps::EntryScope hps_entry_scope_(__func__)
 
 inline hps_status cuda_status(cudaError_t e, const char* what)
 {

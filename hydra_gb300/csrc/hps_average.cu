@@ -211,7 +211,7 @@ size_t hps_average_on_workspace_size(uint64_t n)
 hps_status hps_average_on(const hps_channel* channel, uint64_t first_evt, uint64_t n, const hps_functor* functor,
                           hps_stats* out, void* workspace, size_t workspace_bytes, int32_t precision, void* stream)
 {
-    clear_error();
+    HPS_ENTRY();
     DevChannel ch;
     DevFunctor fn;
     hps_status st = average_args(channel, functor, precision, &ch, &fn);
@@ -244,7 +244,7 @@ hps_status hps_generate_average(const hps_channel* channel, uint64_t first_evt, 
                                 hps_stats* out, void* workspace, size_t workspace_bytes, int32_t precision,
                                 void* stream)
 {
-    clear_error();
+    HPS_ENTRY();
     DevChannel ch;
     DevFunctor fn;
     hps_status st = average_args(channel, functor, precision, &ch, &fn);

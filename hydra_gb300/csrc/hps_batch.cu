@@ -474,7 +474,7 @@ extern "C" {
 hps_status hps_batch_create(hps_batch_plan** out, int32_t max_items, uint64_t max_average_tiles, int32_t precision,
                             const hps_batch_tuning* tuning)
 {
-    clear_error();
+    HPS_ENTRY();
     if (!out) return set_error(HPS_ERR_BAD_ARG, "plan is NULL");
     *out = nullptr;
     if (max_items < 1 || max_items > (1 << 20)) return set_error(HPS_ERR_BAD_ARG, "max_items %d", max_items);
@@ -527,7 +527,7 @@ hps_status hps_batch_create(hps_batch_plan** out, int32_t max_items, uint64_t ma
 
 hps_status hps_batch_set_items(hps_batch_plan* p, const hps_batch_item* items, int32_t n_items, void* stream)
 {
-    clear_error();
+    HPS_ENTRY();
     if (!p) return set_error(HPS_ERR_BAD_ARG, "plan is NULL");
     if (n_items < 0 || n_items > p->max_items)
         return set_error(HPS_ERR_BAD_ARG, "n_items %d outside 0..%d", n_items, p->max_items);
@@ -540,7 +540,7 @@ hps_status hps_batch_set_items(hps_batch_plan* p, const hps_batch_item* items, i
 
 hps_status hps_batch_launch(hps_batch_plan* p, void* stream)
 {
-    clear_error();
+    HPS_ENTRY();
     if (!p) return set_error(HPS_ERR_BAD_ARG, "plan is NULL");
     if (!p->exec) {
         hps_status st = build_graph(p);
@@ -551,7 +551,7 @@ hps_status hps_batch_launch(hps_batch_plan* p, void* stream)
 
 hps_status hps_batch_get_tuning(const hps_batch_plan* p, hps_batch_tuning* out)
 {
-    clear_error();
+    HPS_ENTRY();
     if (!p || !out) return set_error(HPS_ERR_BAD_ARG, "NULL argument");
     *out = p->tuning;
     return HPS_OK;
@@ -559,7 +559,7 @@ hps_status hps_batch_get_tuning(const hps_batch_plan* p, hps_batch_tuning* out)
 
 hps_status hps_batch_set_tuning(hps_batch_plan* p, const hps_batch_tuning* t)
 {
-    clear_error();
+    HPS_ENTRY();
     if (!p || !t) return set_error(HPS_ERR_BAD_ARG, "NULL argument");
     hps_status st = check_tuning(t);
     if (st != HPS_OK) return st;
@@ -577,7 +577,7 @@ hps_status hps_batch_set_tuning(hps_batch_plan* p, const hps_batch_tuning* t)
 
 hps_status hps_batch_autotune(hps_batch_plan* p, void* stream, const char* cache_path, hps_batch_tuning* chosen)
 {
-    clear_error();
+    HPS_ENTRY();
     if (!p) return set_error(HPS_ERR_BAD_ARG, "plan is NULL");
     if (p->n_items == 0) return set_error(HPS_ERR_BAD_ARG, "no items to tune on");
     static std::mutex cache_mu;

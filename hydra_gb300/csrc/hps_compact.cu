@@ -140,10 +140,15 @@ hps_status hps_unweight_compact(int32_t n_daughters, uint64_t n, const double* c
                                 double* weights_out, uint64_t* n_accepted, void* workspace, size_t workspace_bytes,
                                 void* stream)
 {
-    clear_error();
+    HPS_ENTRY();
     if (n_daughters < 2 || n_daughters > HPS_MAX_DAUGHTERS)
         return set_error(HPS_ERR_BAD_ARG, "n_daughters %d outside 2..10", n_daughters);
-    if (n == 0) return HPS_OK;
+    if (n == 0) {
+        // nothing to move; the accepted count is still written (0), in stream order
+        if (!n_accepted) return HPS_OK;
+        return cuda_status(cudaMemsetAsync(n_accepted, 0, sizeof(uint64_t), as_stream(stream)),
+                           "hps_unweight_compact: cudaMemsetAsync(n_accepted)");
+    }
     if (!cols_in || !cols_out || !flags) return set_error(HPS_ERR_BAD_ARG, "cols/flags is NULL");
     if ((weights_in == nullptr) != (weights_out == nullptr))
         return set_error(HPS_ERR_BAD_ARG, "weights_in and weights_out must both be given or both be NULL");

@@ -250,7 +250,7 @@ extern "C" {
 hps_status hps_reweight(int32_t n_daughters, const double* masses, double max_weight, const hps_functor* functor,
                         uint64_t n, const double* const* cols, double* out, double* max_out, void* stream)
 {
-    clear_error();
+    HPS_ENTRY();
     ConstCols cc;
     DevChannel ch;
     hps_status st = stored_event_args(n_daughters, masses, n, cols, &cc, &ch, max_weight);
@@ -274,7 +274,7 @@ hps_status hps_reweight(int32_t n_daughters, const double* masses, double max_we
 hps_status hps_weight_flags(uint64_t n, const double* weights, double max_weight, const double* max_weight_dev,
                             uint64_t unweight_seed, uint64_t first_evt, uint8_t* flags, void* stream)
 {
-    clear_error();
+    HPS_ENTRY();
     if (n == 0) return HPS_OK;
     if (!weights || !flags) return set_error(HPS_ERR_BAD_ARG, "weights/flags is NULL");
     if (!range_ok(first_evt, n)) return set_error(HPS_ERR_BAD_ARG, "event range wraps 2^64");
@@ -288,7 +288,7 @@ hps_status hps_dalitz_histogram(int32_t n_daughters, const double* masses, doubl
                                 const double* const* cols, const double* weights, int32_t weight_mode,
                                 const hps_hist2d* hist, double* bins, void* stream)
 {
-    clear_error();
+    HPS_ENTRY();
     ConstCols cc;
     DevChannel ch;
     hps_status st = stored_event_args(n_daughters, masses, n, cols, &cc, &ch, max_weight);
@@ -317,7 +317,7 @@ hps_status hps_dalitz_histogram(int32_t n_daughters, const double* masses, doubl
 hps_status hps_generate_dalitz(const hps_channel* channel, uint64_t first_evt, uint64_t n, int32_t weight_mode,
                                const hps_hist2d* hist, double* bins, void* stream)
 {
-    clear_error();
+    HPS_ENTRY();
     DevChannel ch;
     hps_status st = to_device_channel(channel, &ch);
     if (st != HPS_OK) return st;

@@ -53,6 +53,7 @@ void to_device_channel_f(const hps_channel* ch, DevChannelF* out)
         out->m[i] = static_cast<float>(ch->masses[i]);
         out->m2[i] = static_cast<float>(ch->masses[i] * ch->masses[i]);
         out->S[i] = static_cast<float>(S);
+        out->S_lo[i] = static_cast<float>(S - static_cast<double>(out->S[i]));
     }
     out->ecm = static_cast<float>(ch->ecm);
     out->ecm_2m64 = static_cast<float>(ch->ecm) * 0x1p-64f;
@@ -188,7 +189,7 @@ uint64_t hps_default_seed(int32_t n, const double* masses)
 hps_status hps_channel_init(hps_channel* ch, int32_t n, int32_t engine, uint64_t seed,
                             double mother_mass, const double* masses, const double* mother)
 {
-    clear_error();
+    HPS_ENTRY();
     if (!ch || !masses) return set_error(HPS_ERR_BAD_ARG, "channel/masses is NULL");
     if (n < 2 || n > HPS_MAX_DAUGHTERS) return set_error(HPS_ERR_BAD_ARG, "n_daughters %d outside 2..10", n);
     if (engine != HPS_ENGINE_PHILOX && engine != HPS_ENGINE_SQUARES3)
@@ -243,7 +244,7 @@ hps_status hps_channel_init(hps_channel* ch, int32_t n, int32_t engine, uint64_t
 hps_status hps_event_weights(int32_t n_daughters, const double* masses, double max_weight, uint64_t n,
                              const double* const* cols, double* out, void* stream)
 {
-    clear_error();
+    HPS_ENTRY();
     ConstCols cc;
     DevChannel ch;
     hps_status st = stored_event_args(n_daughters, masses, n, cols, &cc, &ch, max_weight);
@@ -261,7 +262,7 @@ hps_status hps_unweight_flags(int32_t n_daughters, const double* masses, double 
                               const double* const* cols, uint64_t unweight_seed, uint64_t first_evt,
                               uint8_t* flags, void* stream)
 {
-    clear_error();
+    HPS_ENTRY();
     ConstCols cc;
     DevChannel ch;
     hps_status st = stored_event_args(n_daughters, masses, n, cols, &cc, &ch, max_weight);
@@ -281,7 +282,7 @@ hps_status hps_unweight_flags(int32_t n_daughters, const double* masses, double 
 hps_status hps_rng_words(int32_t n_daughters, int32_t engine, uint64_t seed, uint64_t first_evt, uint64_t n,
                          uint64_t* out, void* stream)
 {
-    clear_error();
+    HPS_ENTRY();
     if (engine != HPS_ENGINE_PHILOX && engine != HPS_ENGINE_SQUARES3)
         return set_error(HPS_ERR_BAD_ARG, "unknown engine %d", engine);
     if (n == 0) return HPS_OK;

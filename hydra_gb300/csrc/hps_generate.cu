@@ -145,7 +145,7 @@ hps_status hps_generate(const hps_channel* channel, uint64_t first_evt, uint64_t
                         double* weights, uint8_t* flags, uint64_t unweight_seed, int32_t precision,
                         void* stream)
 {
-    clear_error();
+    HPS_ENTRY();
     DevChannel ch;
     hps_status st = to_device_channel(channel, &ch);
     if (st != HPS_OK) return st;
@@ -188,7 +188,7 @@ hps_status hps_generate(const hps_channel* channel, uint64_t first_evt, uint64_t
 hps_status hps_evaluate(const hps_channel* channel, uint64_t first_evt, uint64_t n, const hps_functor* functors,
                         int32_t n_functors, double* weights, double* const* out, int32_t precision, void* stream)
 {
-    clear_error();
+    HPS_ENTRY();
     DevChannel ch;
     hps_status st = to_device_channel(channel, &ch);
     if (st != HPS_OK) return st;
@@ -294,7 +294,7 @@ extern "C" hps_status hps_generate_host(const hps_channel* channel, uint64_t fir
                                         uint64_t unweight_seed, int32_t precision, uint64_t chunk_events,
                                         void* stream)
 {
-    clear_error();
+    HPS_ENTRY();
     DevChannel ch;
     hps_status st = to_device_channel(channel, &ch);
     if (st != HPS_OK) return st;
@@ -380,7 +380,7 @@ extern "C" hps_status hps_generate_average_host(const hps_channel* channel, uint
                                                 uint64_t unweight_seed, const hps_functor* functor, hps_stats* out,
                                                 int32_t precision, void* stream)
 {
-    clear_error();
+    HPS_ENTRY();
     DevChannel ch;
     hps_status st = to_device_channel(channel, &ch);
     if (st != HPS_OK) return st;

@@ -206,7 +206,7 @@ extern "C" {
 hps_status hps_generate_mothers(const hps_channel* channel, uint64_t first_evt, uint64_t n, const double* mothers,
                                 double* const* cols, double* weights, int32_t precision, void* stream)
 {
-    clear_error();
+    HPS_ENTRY();
     DevChannel ch;
     hps_status st = mother_args(channel, first_evt, n, mothers, precision, &ch, true);
     if (st != HPS_OK || n == 0) return st;
@@ -244,7 +244,7 @@ hps_status hps_evaluate_mothers(const hps_channel* channel, uint64_t first_evt, 
                                 const hps_functor* functors, int32_t n_functors, double* weights, double* const* out,
                                 int32_t precision, void* stream)
 {
-    clear_error();
+    HPS_ENTRY();
     DevChannel ch;
     hps_status st = mother_args(channel, first_evt, n, mothers, precision, &ch, false);
     if (st != HPS_OK) return st;
@@ -272,7 +272,7 @@ hps_status hps_average_on_mothers(const hps_channel* channel, uint64_t first_evt
                                   const hps_functor* functor, hps_stats* out, void* workspace, size_t workspace_bytes,
                                   int32_t precision, void* stream)
 {
-    clear_error();
+    HPS_ENTRY();
     DevChannel ch;
     hps_status st = mother_args(channel, first_evt, n, mothers, precision, &ch, true);
     if (st != HPS_OK) return st;

@@ -28,7 +28,10 @@ hps_stats* g_noalloc_addr[kMaxDevices] = {};
 
 // Device address of g_noalloc_partials on the current device.  In host code the symbol is
 // only a host-side stand-in, so the address is looked up once per device (with that device
-// current) and cached; the first call on a device does this set-up.
+// current) and cached; the first call on a device does this set-up.  The cache assumes that the
+// device's primary context lives as long as the process: after cudaDeviceReset the module is
+// loaded again, possibly at another address, and the cached one must not be used (a program
+// that resets a device does not call this entry point afterwards).
 hps_status noalloc_scratch(hps_stats** out)
 {
     int dev = 0;
@@ -55,7 +58,7 @@ extern "C" hps_status hps_average_on_noalloc(const hps_channel* channel, uint64_
                                              const hps_functor* functor, hps_stats* out, int32_t precision,
                                              void* stream)
 {
-    clear_error();
+    HPS_ENTRY();
     DevChannel ch;
     DevFunctor fn;
     hps_status st = average_args(channel, functor, precision, &ch, &fn);

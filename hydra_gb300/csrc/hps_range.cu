@@ -34,7 +34,7 @@ extern "C" {
 hps_status hps_range_channel(hps_channel* ch, int32_t n_daughters, const double* masses, const double* mother,
                              uint64_t seed)
 {
-    clear_error();
+    HPS_ENTRY();
     if (!ch || !masses || !mother) return set_error(HPS_ERR_BAD_ARG, "channel/masses/mother is NULL");
     // Vector4R::mass() (hydra/detail/Vector4R.inl:196-209): sqrt(E^2 - p^2) when positive, else 0
     const double m2 = mother[0] * mother[0] - mother[1] * mother[1] - mother[2] * mother[2] - mother[3] * mother[3];
@@ -50,7 +50,7 @@ hps_status hps_range_channel(hps_channel* ch, int32_t n_daughters, const double*
 hps_status hps_generate_range(const hps_channel* channel, uint64_t first_evt, uint64_t n, double* const* cols,
                               double* weights, void* stream)
 {
-    clear_error();
+    HPS_ENTRY();
     if (!channel) return set_error(HPS_ERR_BAD_ARG, "channel is NULL");
     if (channel->engine != HPS_ENGINE_MINSTD)
         return set_error(HPS_ERR_BAD_ARG, "hps_generate_range takes a channel from hps_range_channel");

@@ -311,7 +311,7 @@ extern "C" {
 
 hps_status hps_server_create(hps_server** out, const hps_server_config* cfg)
 {
-    clear_error();
+    HPS_ENTRY();
     if (!out || !cfg) return set_error(HPS_ERR_BAD_ARG, "NULL argument");
     *out = nullptr;
     if (cfg->budget_bytes == 0) return set_error(HPS_ERR_BAD_ARG, "budget_bytes is 0");
@@ -346,7 +346,7 @@ hps_status hps_server_create(hps_server** out, const hps_server_config* cfg)
 
 hps_status hps_server_submit(hps_server* s, const hps_request* req, hps_ticket* ticket)
 {
-    clear_error();
+    HPS_ENTRY();
     if (!s || !req || !ticket) return set_error(HPS_ERR_BAD_ARG, "NULL argument");
     DevChannel dc;
     hps_status st = to_device_channel(&req->channel, &dc);
@@ -381,7 +381,7 @@ hps_status hps_server_submit(hps_server* s, const hps_request* req, hps_ticket* 
 
 hps_status hps_server_poll(hps_server* s, hps_ticket t, hps_result* result, int32_t* done)
 {
-    clear_error();
+    HPS_ENTRY();
     if (!s || !done) return set_error(HPS_ERR_BAD_ARG, "NULL argument");
     std::lock_guard<std::mutex> lock(s->mu);
     auto it = s->reqs.find(t);
@@ -394,7 +394,7 @@ hps_status hps_server_poll(hps_server* s, hps_ticket t, hps_result* result, int3
 
 hps_status hps_server_wait(hps_server* s, hps_ticket t, hps_result* result, double timeout_s)
 {
-    clear_error();
+    HPS_ENTRY();
     if (!s) return set_error(HPS_ERR_BAD_ARG, "NULL argument");
     std::unique_lock<std::mutex> lock(s->mu);
     auto finished = [&] {
@@ -416,7 +416,7 @@ hps_status hps_server_wait(hps_server* s, hps_ticket t, hps_result* result, doub
 
 hps_status hps_server_cancel(hps_server* s, hps_ticket t)
 {
-    clear_error();
+    HPS_ENTRY();
     if (!s) return set_error(HPS_ERR_BAD_ARG, "NULL argument");
     std::lock_guard<std::mutex> lock(s->mu);
     auto it = s->reqs.find(t);
@@ -435,7 +435,7 @@ hps_status hps_server_cancel(hps_server* s, hps_ticket t)
 
 hps_status hps_server_next_done(hps_server* s, hps_ticket* ticket, hps_result* result, double timeout_s)
 {
-    clear_error();
+    HPS_ENTRY();
     if (!s || !ticket) return set_error(HPS_ERR_BAD_ARG, "NULL argument");
     std::unique_lock<std::mutex> lock(s->mu);
     const auto deadline = std::chrono::steady_clock::now() +
@@ -458,7 +458,7 @@ hps_status hps_server_next_done(hps_server* s, hps_ticket* ticket, hps_result* r
 
 hps_status hps_server_release(hps_server* s, hps_ticket t)
 {
-    clear_error();
+    HPS_ENTRY();
     if (!s) return set_error(HPS_ERR_BAD_ARG, "NULL argument");
     std::lock_guard<std::mutex> lock(s->mu);
     auto it = s->reqs.find(t);
@@ -482,7 +482,7 @@ hps_status hps_server_release(hps_server* s, hps_ticket t)
 
 hps_status hps_server_get_stats(hps_server* s, hps_server_stats* out)
 {
-    clear_error();
+    HPS_ENTRY();
     if (!s || !out) return set_error(HPS_ERR_BAD_ARG, "NULL argument");
     std::lock_guard<std::mutex> lock(s->mu);
     *out = s->st;

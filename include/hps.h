@@ -208,7 +208,9 @@ hps_status hps_generate_average_host(const hps_channel* ch, uint64_t first_evt, 
  * exits.  Limits and rules:
  *  - n above HPS_NOALLOC_MAX_EVENTS (2^26 events) is rejected with HPS_ERR_BAD_ARG;
  *  - the first call on each device looks up the array's device address (with that device
- *    current) and caches it; make that first call before any stream capture on the device;
+ *    current) and caches it; make that first call before any stream capture on the device; the
+ *    cache assumes the device's primary context lives until the process exits (no
+ *    cudaDeviceReset of that device between calls);
  *  - all calls share the one array, so calls that overlap on the GPU (different streams, or
  *    different host threads, on the same device) race and must be serialised by the caller;
  *  - nothing in the array needs clearing between calls: each call writes every entry it reads. */

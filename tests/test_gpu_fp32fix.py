@@ -26,6 +26,10 @@ CASES = [
     ("n4_sq", 4, 1, 3.0, [0.1, 0.2, 0.3, 0.4]),
     ("n7_mixed", 7, 1, 6.0, [PI, K, 0.938272, PI, PI, K, PI]),
     ("n6_threshold", 6, 0, 6 * PI + 1e-3, [PI] * 6),
+    ("n8_pions", 8, 0, 3.0, [PI] * 8),
+    ("n8_sq_mixed", 8, 1, 4.5, [K, PI, 0.938272, PI, PI, K, PI, PI]),
+    ("n9_pions", 9, 0, 3.0, [PI] * 9),
+    ("n9_sq_mixed", 9, 1, 5.0, [PI, K, PI, 0.938272, PI, PI, K, PI, PI]),
 ]
 
 
@@ -60,7 +64,7 @@ def errors(api, torch, oracle, N, engine, M, masses, n, seed=0x3039, first=0):
 
 @pytest.mark.parametrize("name,N,engine,M,masses", CASES)
 def test_fp32fix_generate_max_relative_error(api, torch, oracle, name, N, engine, M, masses):
-    n = 1 << 20
+    n = (1 << 20) + (77 if N in (8, 9) else 0)        # N = 8, 9: a ragged last chunk
     e4, ew, fl, rw, och = errors(api, torch, oracle, N, engine, M, masses, n)
     print(f"\n[fp32_fix] {name}: max four-vector err {e4:.3e}, max weight err {ew:.3e}")
     assert e4 <= TOL, e4

@@ -367,3 +367,18 @@ def test_unweight_compact_is_stable_partition(api, torch, oracle, n):
     assert int(nacc.item()) == int(fl.sum())
     assert np.array_equal(out.cpu().numpy(), four[:, order])
     assert np.array_equal(wout.cpu().numpy(), w[order])
+
+
+def test_unweight_compact_empty_writes_zero_count(api, torch):
+    """n = 0 moves nothing and still writes the accepted count (0) to the caller's buffer."""
+    tf = torch.empty((5, 0, 4), dtype=torch.float64, device="cuda")
+    tfl = torch.empty(0, dtype=torch.uint8, device="cuda")
+    nacc = torch.full((1,), 12345, dtype=torch.int64, device="cuda")
+    cin = api._ptr_array([tf[k] for k in range(5)])
+    cout = api._ptr_array([tf[k] for k in range(5)])
+    st = api.lib().hps_unweight_compact(5, 0, api.ctypes.cast(cin, api.ctypes.c_void_p), None, api._dptr(tfl),
+                                        api.ctypes.cast(cout, api.ctypes.c_void_p), None, api._dptr(nacc), None, 0,
+                                        None)
+    assert st == 0
+    torch.cuda.synchronize()
+    assert int(nacc.item()) == 0

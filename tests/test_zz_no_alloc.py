@@ -73,3 +73,25 @@ def test_noalloc_rejects_oversized_request(hps, api):
     assert b"allocation-free limit" in hps.lib().hps_last_error()
     torch.cuda.synchronize()
     assert out.cpu().tolist() == [0.0, 0.0, 0.0]       # nothing was launched
+
+
+def test_noalloc_at_the_limit_and_empty(hps, api):
+    """n exactly HPS_NOALLOC_MAX_EVENTS writes and reads the last entry of the array; n = 0
+    launches no tile and returns an empty StatsPHSP."""
+    import torch
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    limit = 16384 * 4096
+    ch = api.make_channel([K, PI, PI, PI, PI], 1.86484, 0x3039, "philox")
+    fn = api.functor_bw2(0, 1, 0.8955, 0.0473)
+    got = torch.zeros(3, dtype=torch.float64, device="cuda")
+    ref = torch.zeros(3, dtype=torch.float64, device="cuda")
+    assert _noalloc(hps, ch, 7, limit, fn, got, 1, stream) == hps.OK, hps.lib().hps_last_error()
+    assert _allocating(hps, ch, 7, limit, fn, ref, 1, stream) == hps.OK, hps.lib().hps_last_error()
+    torch.cuda.synchronize()
+    g, r = got.cpu().tolist(), ref.cpu().tolist()
+    assert r[2] > 0 and _close(g, r), (g, r)
+    for precision in (0, 1):
+        out = torch.full((3,), 7.0, dtype=torch.float64, device="cuda")
+        assert _noalloc(hps, ch, 0, 0, fn, out, precision, stream) == hps.OK, hps.lib().hps_last_error()
+        torch.cuda.synchronize()
+        assert out.cpu().tolist() == [0.0, 0.0, 0.0]
