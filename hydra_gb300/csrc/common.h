@@ -44,6 +44,9 @@ hps_status to_device_channel(const hps_channel* ch, DevChannel* out);
 hps_status to_device_functor(const hps_functor* f, int n_daughters, DevFunctor* out);
 // Float-side constants for the FP32_FIX kernels (prefix sums formed in double, then rounded).
 void to_device_channel_f(const hps_channel* ch, DevChannelF* out);
+// Whether the FP32_FIX kernels take the float-float boosts for this channel (N at least
+// f32::kPreciseN, or at least f32::kHardMinN with ECM >= f32::kHardRatio x the lightest mass).
+bool float_float_form(const hps_channel* ch);
 
 // AverageOn pieces shared by its entry points (hps_average.cu): host-side validation that
 // touches no device state, and the tile + final-merge launches into caller-provided partials.
@@ -96,6 +99,26 @@ inline unsigned grid_for(uint64_t items, unsigned threads, unsigned max_ctas = 1
     case 8:  BODY(4, 0)  break; case 9:  BODY(4, 1)  break;                     \
     case 10: BODY(5, 0)  break; case 11: BODY(5, 1)  break;                     \
     case 12: BODY(6, 0)  break; case 13: BODY(6, 1)  break;                     \
+    case 14: BODY(7, 0)  break; case 15: BODY(7, 1)  break;                     \
+    case 16: BODY(8, 0)  break; case 17: BODY(8, 1)  break;                     \
+    case 18: BODY(9, 0)  break; case 19: BODY(9, 1)  break;                     \
+    case 20: BODY(10, 0) break; case 21: BODY(10, 1) break;                     \
+    default: return set_error(HPS_ERR_BAD_ARG, "n_daughters %d outside 2..10", (int)(n_daughters)); \
+    }
+
+// The same for the FP32_FIX kernels: a channel whose float-side constants ask for the float-float
+// boosts (DevChannelF::precise, N = 4..6; from N = 7 on they are always taken) gets the
+// instantiation with kPreciseForm in its ENGINE parameter.
+#define HPS_DISPATCH_F32(n_daughters, engine, precise, BODY)                    \
+    switch ((n_daughters) * 2 + ((engine) == 0 ? 0 : 1)) {                      \
+    case 4:  BODY(2, 0)  break; case 5:  BODY(2, 1)  break;                     \
+    case 6:  BODY(3, 0)  break; case 7:  BODY(3, 1)  break;                     \
+    case 8:  if (precise) { BODY(4, 4) } else { BODY(4, 0) } break;             \
+    case 9:  if (precise) { BODY(4, 5) } else { BODY(4, 1) } break;             \
+    case 10: if (precise) { BODY(5, 4) } else { BODY(5, 0) } break;             \
+    case 11: if (precise) { BODY(5, 5) } else { BODY(5, 1) } break;             \
+    case 12: if (precise) { BODY(6, 4) } else { BODY(6, 0) } break;             \
+    case 13: if (precise) { BODY(6, 5) } else { BODY(6, 1) } break;             \
     case 14: BODY(7, 0)  break; case 15: BODY(7, 1)  break;                     \
     case 16: BODY(8, 0)  break; case 17: BODY(8, 1)  break;                     \
     case 18: BODY(9, 0)  break; case 19: BODY(9, 1)  break;                     \

@@ -10,6 +10,7 @@
 // (CUDA's sincos versus the host libm).
 #pragma once
 #include <cstdint>
+#include "../../include/hps.h"
 #include "rng.cuh"
 
 namespace hps {
@@ -23,6 +24,20 @@ struct DevChannel {
     uint64_t key;         // splitmix64(seed): Philox key / squares3 key
     int boost_active;     // 0 < |beta|^2 < 1: only then does applyBoostTo change anything
 };
+
+// Host side: the kernel-side form of a validated channel (the reference's functor members:
+// masses, ECM, max weight, final-boost vector; the engine key splitmix64(seed)).
+inline void make_channel(const hps_channel& c, DevChannel& out)
+{
+    out = DevChannel{};
+    for (int i = 0; i < c.n_daughters && i < 10; ++i) out.masses[i] = c.masses[i];
+    out.ecm = c.ecm;
+    out.max_weight = c.max_weight;
+    for (int k = 0; k < 3; ++k) out.beta[k] = c.beta[k];
+    out.key = splitmix64(c.seed);
+    const double b2 = c.beta[0] * c.beta[0] + c.beta[1] * c.beta[1] + c.beta[2] * c.beta[2];
+    out.boost_active = (b2 > 0.0 && b2 < 1.0) ? 1 : 0;
+}
 
 namespace f64 {
 

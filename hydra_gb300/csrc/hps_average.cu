@@ -169,7 +169,7 @@ hps_status launch_average(const hps_channel* channel, const DevChannel& ch, cons
             else                                                                                   \
                 k_average_tiles_f32fix<NN, EE><<<grid, kAvgThreads, 0, stream>>>(ch, chf, fn, first_evt, n, \
                                                                                   ntiles, partials, k0);
-            HPS_DISPATCH_N_ENGINE(channel->n_daughters, channel->engine, HPS_BODY)
+            HPS_DISPATCH_F32(channel->n_daughters, channel->engine, chf.precise, HPS_BODY)
 #undef HPS_BODY
         } else {
 #define HPS_BODY(NN, EE)                                                                          \
@@ -188,7 +188,7 @@ hps_status launch_average(const hps_channel* channel, const DevChannel& ch, cons
         to_device_channel_f(channel, &chf);
 #define HPS_BODY(NN, EE)                                                                                   \
         k_average_final_f32fix<NN, EE><<<1, kFinalThreads, 0, stream>>>(ch, chf, fn, first_evt, partials, ntiles, out);
-        HPS_DISPATCH_N_ENGINE(channel->n_daughters, channel->engine, HPS_BODY)
+        HPS_DISPATCH_F32(channel->n_daughters, channel->engine, chf.precise, HPS_BODY)
 #undef HPS_BODY
     } else {
         k_average_final<<<1, kFinalThreads, 0, stream>>>(partials, ntiles, out);

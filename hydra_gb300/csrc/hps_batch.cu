@@ -41,13 +41,25 @@ struct BatchItemDev {
     int32_t mode, N, engine, vec32;
 };
 
-// Register classes: one per N (class c holds N = c + 2).  Each class kernel carries both engines
-// and both modes of its N; ptxas gives them 60 (N = 2) to 128 (N = 9, 10) registers, against 128
-// for a kernel over every N.
-constexpr int kBatchClasses = 9;
-__host__ __device__ constexpr int class_lo(int c) { return c + 2; }
-__host__ __device__ constexpr int class_hi(int c) { return c + 2; }
-inline int batch_class(int N) { return N < 2 ? 0 : N > 10 ? kBatchClasses - 1 : N - 2; }
+// (N = 7 and 8 were once capped at 80 registers for 3 CTAs per SM; with the float-float weight and
+// boosts that cap spills 184 and 356 bytes per thread, so every class runs uncapped.)
+// Register classes: one per N (class c < 9 holds N = c + 2), and for N = 4..6 one more each for
+// the channels that take the float-float boosts (classes 9..11: N = c - 5), which need more
+// registers than the plain form of the same N.  Each class kernel carries both engines and both
+// modes of its N; ptxas gives them 60 (N = 2) to 128 (N = 9, 10) registers, against 128 for a
+// kernel over every N.
+constexpr int kBatchClasses = 12;
+__host__ __device__ constexpr int class_n(int c) { return c < 9 ? c + 2 : c - 5; }
+__host__ __device__ constexpr bool class_ff(int c) { return c >= 9; }
+inline bool ff_class_n(int N) { return N >= f32::kHardMinN && N < f32::kPreciseN; }
+inline int batch_class(int N, bool ff)
+{
+    if (N < 2) return 0;
+    if (N > 10) return 8;
+    return (ff && ff_class_n(N)) ? N + 5 : N - 2;
+}
+// The engine field of a table entry: the engine, with kPreciseForm for the float-float classes.
+inline int item_engine(int N, int engine, bool ff) { return engine | ((ff && ff_class_n(N)) ? kPreciseForm : 0); }
 
 struct BatchHeader {
     // next unit of each class, relative; the last one serves the single kernel over every N
@@ -83,7 +95,7 @@ __device__ __forceinline__ void batch_body(const BatchItemDev* __restrict__ item
                                            hps_stats* __restrict__ partials)
 {
     // largest shared-memory word exchange of the class (Philox at its largest N)
-    __shared__ __align__(16) unsigned char smem[WordShare<class_hi(CLS), kPhilox, kTileThreads>::BYTES2];
+    __shared__ __align__(16) unsigned char smem[WordShare<class_n(CLS), kPhilox, kTileThreads>::BYTES2];
     __shared__ unsigned long long s_unit;
     __shared__ int s_item;
     // The unit's item, staged in shared memory: the channel constants are then re-read after the
@@ -119,15 +131,23 @@ __device__ __forceinline__ void batch_body(const BatchItemDev* __restrict__ item
         __syncthreads();                                  // s_it staged; s_unit / s_item read before they change
         const BatchItemDev& it = s_it;
         const uint64_t lu = u - it.unit_begin;
-        switch (it.N * 2 + it.engine) {
+        switch (it.N * 8 + it.engine) {
 #define HPS_UNIT(NN)                                                                             \
-        case NN * 2 + 0:                                                                         \
-            if constexpr (NN >= class_lo(CLS) && NN <= class_hi(CLS))                            \
+        case NN * 8 + 0:                                                                         \
+            if constexpr (NN == class_n(CLS) && !class_ff(CLS))                                  \
                 run_unit<NN, kPhilox>(it, lu, store_tile, partials, smem);                       \
             break;                                                                               \
-        case NN * 2 + 1:                                                                         \
-            if constexpr (NN >= class_lo(CLS) && NN <= class_hi(CLS))                            \
+        case NN * 8 + 1:                                                                         \
+            if constexpr (NN == class_n(CLS) && !class_ff(CLS))                                  \
                 run_unit<NN, kSquares3>(it, lu, store_tile, partials, smem);                     \
+            break;                                                                               \
+        case NN * 8 + kPreciseForm:                                                              \
+            if constexpr (NN == class_n(CLS) && class_ff(CLS))                                   \
+                run_unit<NN, kPhilox | kPreciseForm>(it, lu, store_tile, partials, smem);        \
+            break;                                                                               \
+        case NN * 8 + (kSquares3 | kPreciseForm):                                                \
+            if constexpr (NN == class_n(CLS) && class_ff(CLS))                                   \
+                run_unit<NN, kSquares3 | kPreciseForm>(it, lu, store_tile, partials, smem);      \
             break;
         HPS_UNIT(2) HPS_UNIT(3) HPS_UNIT(4) HPS_UNIT(5) HPS_UNIT(6) HPS_UNIT(7) HPS_UNIT(8) HPS_UNIT(9)
         HPS_UNIT(10)
@@ -140,15 +160,6 @@ __device__ __forceinline__ void batch_body(const BatchItemDev* __restrict__ item
 template <int CLS>
 __global__ void __launch_bounds__(kTileThreads)
 k_batch_f32(const BatchItemDev* __restrict__ items, BatchHeader* __restrict__ hdr, hps_stats* __restrict__ partials)
-{
-    batch_body<CLS>(items, hdr, partials);
-}
-
-// N = 7 and 8 capped at 80 registers (3 CTAs per SM instead of 2, a few bytes of spill):
-// 0.74 / 0.90 ms against 0.81 / 0.95 ms for one 2^23-event channel in the batch.
-template <int CLS>
-__global__ void __launch_bounds__(kTileThreads, 3)
-k_batch_f32_3(const BatchItemDev* __restrict__ items, BatchHeader* __restrict__ hdr, hps_stats* __restrict__ partials)
 {
     batch_body<CLS>(items, hdr, partials);
 }
@@ -184,12 +195,17 @@ k_batch_f32_all(const BatchItemDev* __restrict__ items, BatchHeader* __restrict_
         if (u >= total) return;
         const BatchItemDev& it = items[item];
         const uint64_t lu = u - it.unit_begin;
-        switch (it.N * 2 + it.engine) {
+        switch (it.N * 8 + it.engine) {
 #define HPS_UNIT(NN)                                                                         \
-        case NN * 2 + 0: run_unit<NN, kPhilox>(it, lu, store_tile, partials, smem); break;   \
-        case NN * 2 + 1: run_unit<NN, kSquares3>(it, lu, store_tile, partials, smem); break;
-        HPS_UNIT(2) HPS_UNIT(3) HPS_UNIT(4) HPS_UNIT(5) HPS_UNIT(6) HPS_UNIT(7) HPS_UNIT(8) HPS_UNIT(9)
+        case NN * 8 + 0: run_unit<NN, kPhilox>(it, lu, store_tile, partials, smem); break;   \
+        case NN * 8 + 1: run_unit<NN, kSquares3>(it, lu, store_tile, partials, smem); break;
+#define HPS_UNIT_FF(NN)                                                                      \
+        HPS_UNIT(NN)                                                                         \
+        case NN * 8 + 4: run_unit<NN, kPhilox | kPreciseForm>(it, lu, store_tile, partials, smem); break; \
+        case NN * 8 + 5: run_unit<NN, kSquares3 | kPreciseForm>(it, lu, store_tile, partials, smem); break;
+        HPS_UNIT(2) HPS_UNIT(3) HPS_UNIT_FF(4) HPS_UNIT_FF(5) HPS_UNIT_FF(6) HPS_UNIT(7) HPS_UNIT(8) HPS_UNIT(9)
         HPS_UNIT(10)
+#undef HPS_UNIT_FF
 #undef HPS_UNIT
         default: break;
         }
@@ -204,12 +220,17 @@ __global__ void k_batch_shift(const BatchItemDev* __restrict__ items, const Batc
     const BatchItemDev& it = items[blockIdx.x];
     if (it.mode != HPS_MODE_AVERAGE || it.n == 0) return;
     float K0 = 0.0f;
-    switch (it.N * 2 + it.engine) {
+    switch (it.N * 8 + it.engine) {
 #define HPS_SHIFT(NN)                                                                          \
-    case NN * 2 + 0: K0 = call_shift<NN, kPhilox>(it.chd, it.chf, it.fn, it.first); break;     \
-    case NN * 2 + 1: K0 = call_shift<NN, kSquares3>(it.chd, it.chf, it.fn, it.first); break;
-    HPS_SHIFT(2) HPS_SHIFT(3) HPS_SHIFT(4) HPS_SHIFT(5) HPS_SHIFT(6) HPS_SHIFT(7) HPS_SHIFT(8) HPS_SHIFT(9)
+    case NN * 8 + 0: K0 = call_shift<NN, kPhilox>(it.chd, it.chf, it.fn, it.first); break;     \
+    case NN * 8 + 1: K0 = call_shift<NN, kSquares3>(it.chd, it.chf, it.fn, it.first); break;
+#define HPS_SHIFT_FF(NN)                                                                                  \
+    HPS_SHIFT(NN)                                                                                         \
+    case NN * 8 + 4: K0 = call_shift<NN, kPhilox | kPreciseForm>(it.chd, it.chf, it.fn, it.first); break;  \
+    case NN * 8 + 5: K0 = call_shift<NN, kSquares3 | kPreciseForm>(it.chd, it.chf, it.fn, it.first); break;
+    HPS_SHIFT(2) HPS_SHIFT(3) HPS_SHIFT_FF(4) HPS_SHIFT_FF(5) HPS_SHIFT_FF(6) HPS_SHIFT(7) HPS_SHIFT(8) HPS_SHIFT(9)
     HPS_SHIFT(10)
+#undef HPS_SHIFT_FF
 #undef HPS_SHIFT
     default: break;
     }
@@ -227,11 +248,11 @@ k_batch_merge(const BatchItemDev* __restrict__ items, const BatchHeader* __restr
     // every thread reads K0 before the block reduction's barriers; thread 0 writes the stats after them
     const float K0 = it.units ? *reinterpret_cast<const float*>(it.stats) : 0.0f;
     hps_stats r{0.0, 0.0, 0.0};
-    switch (it.N * 2 + it.engine) {
+    switch (it.N * 8 + engine_of(it.engine)) {     // the merge does not depend on the form
 #define HPS_MERGE(NN)                                                                                        \
-    case NN * 2 + 0: r = merge_sums<NN, kPhilox>(it.chd, it.chf, it.fn, it.first, partials + it.partial_offset,  \
+    case NN * 8 + 0: r = merge_sums<NN, kPhilox>(it.chd, it.chf, it.fn, it.first, partials + it.partial_offset,  \
                                                  it.units, K0); break;                                        \
-    case NN * 2 + 1: r = merge_sums<NN, kSquares3>(it.chd, it.chf, it.fn, it.first,                            \
+    case NN * 8 + 1: r = merge_sums<NN, kSquares3>(it.chd, it.chf, it.fn, it.first,                            \
                                                    partials + it.partial_offset, it.units, K0); break;
     HPS_MERGE(2) HPS_MERGE(3) HPS_MERGE(4) HPS_MERGE(5) HPS_MERGE(6) HPS_MERGE(7) HPS_MERGE(8) HPS_MERGE(9)
     HPS_MERGE(10)
@@ -246,8 +267,9 @@ typedef void (*BatchKernel)(const BatchItemDev*, BatchHeader*, hps_stats*);
 inline BatchKernel class_kernel(int c)
 {
     static const BatchKernel k[kBatchClasses] = {k_batch_f32<0>, k_batch_f32<1>, k_batch_f32<2>,
-                                                 k_batch_f32<3>, k_batch_f32<4>, k_batch_f32_3<5>,
-                                                 k_batch_f32_3<6>, k_batch_f32<7>, k_batch_f32<8>};
+                                                 k_batch_f32<3>, k_batch_f32<4>, k_batch_f32<5>,
+                                                 k_batch_f32<6>, k_batch_f32<7>, k_batch_f32<8>,
+                                                 k_batch_f32<9>, k_batch_f32<10>, k_batch_f32<11>};
     return k[c];
 }
 
@@ -384,16 +406,19 @@ hps_status upload_items(hps_batch_plan* p, const std::vector<hps_batch_item>& it
     // rejected below, wherever it sorts)
     std::vector<int> order(n_items);
     int32_t item_begin[kBatchClasses + 1] = {};
-    for (int i = 0; i < n_items; ++i) ++item_begin[batch_class(items[i].channel.n_daughters) + 1];
+    auto cls = [&](int i) {
+        return batch_class(items[i].channel.n_daughters, float_float_form(&items[i].channel));
+    };
+    for (int i = 0; i < n_items; ++i) ++item_begin[cls(i) + 1];
     for (int c = 0; c < kBatchClasses; ++c) item_begin[c + 1] += item_begin[c];
     {
         int32_t next[kBatchClasses];
         for (int c = 0; c < kBatchClasses; ++c) next[c] = item_begin[c];
-        for (int i = 0; i < n_items; ++i) order[next[batch_class(items[i].channel.n_daughters)]++] = i;
+        for (int i = 0; i < n_items; ++i) order[next[cls(i)]++] = i;
     }
     uint64_t class_begin[kBatchClasses + 1] = {};
     uint64_t unit = 0, partial = 0, events = 0;
-    std::vector<int> mix(2 * 11 * 2, 0);
+    std::vector<int> mix(2 * 11 * 8, 0);
     for (int pos = 0, c = 0; pos < n_items; ++pos) {
         while (c < kBatchClasses && pos == item_begin[c + 1]) class_begin[++c] = unit;
         const int i = order[pos];
@@ -406,7 +431,7 @@ hps_status upload_items(hps_batch_plan* p, const std::vector<hps_batch_item>& it
         if (!range_ok(in.first_evt, in.n_events)) return set_error(HPS_ERR_BAD_ARG, "item %d: event range wraps", i);
         const int N = in.channel.n_daughters;
         d.N = N;
-        d.engine = in.channel.engine;
+        d.engine = item_engine(N, in.channel.engine, d.chf.precise != 0);
         d.mode = in.mode;
         d.first = in.first_evt;
         d.n = in.n_events;
@@ -441,7 +466,7 @@ hps_status upload_items(hps_batch_plan* p, const std::vector<hps_batch_item>& it
         }
         unit += d.units;
         events += in.n_events;
-        mix[(in.mode * 11 + N) * 2 + d.engine] += 1;
+        mix[(in.mode * 11 + N) * 8 + d.engine] += 1;
     }
     for (int c = 0; c < kBatchClasses; ++c) {
         // classes after the last item's (and every class of an empty table) end at the last unit

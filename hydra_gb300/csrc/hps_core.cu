@@ -33,59 +33,13 @@ hps_status to_device_channel(const hps_channel* ch, DevChannel* out)
         return set_error(HPS_ERR_BAD_ARG, "HPS_ENGINE_MINSTD channels are for hps_generate_range only");
     if (ch->engine != HPS_ENGINE_PHILOX && ch->engine != HPS_ENGINE_SQUARES3)
         return set_error(HPS_ERR_BAD_ARG, "unknown engine %d", ch->engine);
-    std::memset(out, 0, sizeof(*out));
-    for (int i = 0; i < ch->n_daughters; ++i) out->masses[i] = ch->masses[i];
-    out->ecm = ch->ecm;
-    out->max_weight = ch->max_weight;
-    for (int c = 0; c < 3; ++c) out->beta[c] = ch->beta[c];
-    out->key = splitmix64(ch->seed);
-    const double b2 = ch->beta[0] * ch->beta[0] + ch->beta[1] * ch->beta[1] + ch->beta[2] * ch->beta[2];
-    out->boost_active = (b2 > 0.0 && b2 < 1.0) ? 1 : 0;
+    make_channel(*ch, *out);
     return HPS_OK;
 }
 
-void to_device_channel_f(const hps_channel* ch, DevChannelF* out)
-{
-    std::memset(out, 0, sizeof(*out));
-    double S = 0.0;
-    for (int i = 0; i < ch->n_daughters; ++i) {
-        S += ch->masses[i];
-        out->m[i] = static_cast<float>(ch->masses[i]);
-        out->m2[i] = static_cast<float>(ch->masses[i] * ch->masses[i]);
-        out->S[i] = static_cast<float>(S);
-        out->S_lo[i] = static_cast<float>(S - static_cast<double>(out->S[i]));
-    }
-    out->ecm = static_cast<float>(ch->ecm);
-    out->ecm_2m64 = static_cast<float>(ch->ecm) * 0x1p-64f;
-    for (int i = 0; i < ch->n_daughters; ++i) {
-        const double m2x = 2.0 * ch->masses[i];
-        out->m2x_hi[i] = static_cast<float>(m2x);
-        out->m2x_lo[i] = static_cast<float>(m2x - static_cast<double>(out->m2x_hi[i]));
-    }
-    const double e64 = ch->ecm * 0x1p-64;
-    out->e64_hi = static_cast<float>(e64);
-    out->e64_lo = static_cast<float>(e64 - static_cast<double>(out->e64_hi));
-    // Stage n (pd of daughter n+1) is largest at a = emmax = ECM + m_0..m_{n+1}, b = emmin =
-    // m_0..m_n: num = (2a pd)^2 <= (2 emmax pdmax)^2 and 2a <= 2 emmax.  Both are scaled by powers
-    // of two to about 1 there; w_exp = sum(num exponents)/2 - sum(2a exponents) undoes it.
-    double emmax = ch->ecm + ch->masses[0], emmin = 0.0;
-    int w_exp = 0;
-    for (int n = 0; n + 1 < ch->n_daughters && n < 9; ++n) {
-        emmin += ch->masses[n];
-        emmax += ch->masses[n + 1];
-        const double a = emmax, b = emmin, c = ch->masses[n + 1];
-        const double pdmax = std::sqrt((a - b - c) * (a + b + c) * (a - b + c) * (a + b - c)) / (2 * a);
-        const double num_max = (2 * a * pdmax) * (2 * a * pdmax);
-        int e_num = 0, e_a2 = 0;
-        std::frexp(num_max, &e_num);
-        std::frexp(2 * a, &e_a2);
-        const int half = (num_max > 0.0) ? e_num / 2 : 0;       // num scaled by 4^-half
-        out->num_scale[n] = std::ldexp(1.0f, -2 * half);
-        out->a2_scale[n] = std::ldexp(1.0f, -e_a2);
-        w_exp += half - e_a2;
-    }
-    out->w_exp = w_exp;
-}
+void to_device_channel_f(const hps_channel* ch, DevChannelF* out) { f32::make_channel_f(*ch, *out); }
+
+bool float_float_form(const hps_channel* ch) { return f32::float_float_form(*ch); }
 
 hps_status to_device_functor(const hps_functor* f, int n_daughters, DevFunctor* out)
 {

@@ -173,7 +173,7 @@ hps_status hps_generate(const hps_channel* channel, uint64_t first_evt, uint64_t
 #define HPS_BODY(NN, EE)                                                                         \
         k_generate_f32fix<NN, EE><<<grid_for(n, gen_events_per_iteration(NN), kGenMaxCtas), gen_threads(NN), 0, as_stream(stream)>>>(ch, chf, cc, weights, flags, ukey, \
                                                                         first_evt, n, vec32);
-        HPS_DISPATCH_N_ENGINE(N, channel->engine, HPS_BODY)
+        HPS_DISPATCH_F32(N, channel->engine, chf.precise, HPS_BODY)
 #undef HPS_BODY
     } else {
 #define HPS_BODY(NN, EE)                                                                  \
@@ -214,7 +214,7 @@ hps_status hps_evaluate(const hps_channel* channel, uint64_t first_evt, uint64_t
 #define HPS_BODY(NN, EE)                                                                           \
         k_evaluate_f32fix<NN, EE><<<grid, kGenThreads, 0, as_stream(stream)>>>(ch, chf, fs, n_functors, weights, \
                                                                         oc, first_evt, n);
-        HPS_DISPATCH_N_ENGINE(N, channel->engine, HPS_BODY)
+        HPS_DISPATCH_F32(N, channel->engine, chf.precise, HPS_BODY)
 #undef HPS_BODY
     } else {
 #define HPS_BODY(NN, EE)                                                                          \

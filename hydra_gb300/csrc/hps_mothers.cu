@@ -228,7 +228,7 @@ hps_status hps_generate_mothers(const hps_channel* channel, uint64_t first_evt, 
 #define HPS_BODY(NN, EE)                                                                                 \
         k_generate_mothers_f32fix<NN, EE><<<grid, kTileThreads, 0, as_stream(stream)>>>(ch, chf, mothers, c32, \
                                                                                      weights, first_evt, n, all32 ? 1 : 0);
-        HPS_DISPATCH_N_ENGINE(N, channel->engine, HPS_BODY)
+        HPS_DISPATCH_F32(N, channel->engine, chf.precise, HPS_BODY)
 #undef HPS_BODY
         return cuda_status(cudaGetLastError(), "hps_generate_mothers launch");
     }
@@ -308,7 +308,7 @@ hps_status hps_average_on_mothers(const hps_channel* channel, uint64_t first_evt
                                                                                  partials, k0, mothers);        \
         }                                                                                                       \
         k_average_mothers_final_f32fix<NN, EE><<<1, kFinalThreads, 0, s>>>(ch, chf, fn, first_evt, partials, ntiles, out);
-        HPS_DISPATCH_N_ENGINE(channel->n_daughters, channel->engine, HPS_BODY)
+        HPS_DISPATCH_F32(channel->n_daughters, channel->engine, chf.precise, HPS_BODY)
 #undef HPS_BODY
     } else {
         if (ntiles) {

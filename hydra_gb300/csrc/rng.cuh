@@ -21,6 +21,12 @@ namespace hps {
 
 enum : int { kPhilox = 0, kSquares3 = 1, kMinstd = 2 };
 
+// The FP32_FIX kernels carry one more compile-time choice in their ENGINE parameter: bit
+// kPreciseForm selects the float-float boosts of the event body (genbod_f32.cuh, event_body).
+// The random streams depend only on engine_of(ENGINE).
+constexpr int kPreciseForm = 4;
+__host__ __device__ constexpr int engine_of(int e) { return e & 3; }
+
 // minstd_rand arithmetic modulo the Mersenne prime 2^31 - 1: x < 2^62 folds as
 // (x mod 2^31) + (x >> 31), twice, then one conditional subtraction; exact.
 constexpr uint32_t kLcgA = 48271u;
@@ -98,7 +104,7 @@ template <int N, int ENGINE>
 __device__ __forceinline__ void stream_words(uint64_t key, uint64_t base, uint64_t (&w)[3 * N - 4])
 {
     constexpr int NW = 3 * N - 4;
-    if constexpr (ENGINE == kPhilox) {
+    if constexpr (engine_of(ENGINE) == kPhilox) {
         constexpr int NB = (NW + 1) / 2;
 #pragma unroll
         for (int b = 0; b < NB; ++b) {
@@ -109,7 +115,7 @@ __device__ __forceinline__ void stream_words(uint64_t key, uint64_t base, uint64
             w[2 * b] = o0;
             if (2 * b + 1 < NW) w[2 * b + 1] = o1;
         }
-    } else if constexpr (ENGINE == kMinstd) {
+    } else if constexpr (engine_of(ENGINE) == kMinstd) {
         // key = seeded state; the first draw after discard(base) is state * 48271^(base+1)
         uint32_t x = lcg_mulmod(static_cast<uint32_t>(key), lcg_pow(base + 1u));
         w[0] = x;
@@ -134,8 +140,8 @@ __device__ __forceinline__ void event_words(uint64_t key, uint64_t evt, uint64_t
 template <int ENGINE>
 __device__ __forceinline__ double word_to_uniform(uint64_t x)
 {
-    if constexpr (ENGINE == kPhilox) return __ull2double_rn(x) * 0x1p-64;
-    else if constexpr (ENGINE == kMinstd)
+    if constexpr (engine_of(ENGINE) == kPhilox) return __ull2double_rn(x) * 0x1p-64;
+    else if constexpr (engine_of(ENGINE) == kMinstd)
         return __ddiv_rn(static_cast<double>(static_cast<uint32_t>(x) - 1u), 2147483646.0);
     else return static_cast<double>(static_cast<uint32_t>(x)) * 0x1p-32;
 }
@@ -176,9 +182,9 @@ namespace hps {
 
 template <int N, int ENGINE, int NT> struct WordShare {
     static constexpr int NW = 3 * N - 4;
-    static constexpr int B = (ENGINE == kPhilox) ? (NW + 1) / 2 : NW;   // items per event
+    static constexpr int B = (engine_of(ENGINE) == kPhilox) ? (NW + 1) / 2 : NW;   // items per event
     static constexpr int SLOTS = NT + B - 1;
-    static constexpr int BYTES = SLOTS * ((ENGINE == kPhilox) ? 16 : 8);
+    static constexpr int BYTES = SLOTS * ((engine_of(ENGINE) == kPhilox) ? 16 : 8);
     static constexpr int BYTES2 = 2 * BYTES;                            // two buffers, see below
 };
 
@@ -196,7 +202,7 @@ __device__ __forceinline__ void cta_event_words(uint64_t key, uint64_t e0, void*
     using S = WordShare<N, ENGINE, NT>;
     const int t = threadIdx.x;
     smem = static_cast<unsigned char*>(smem) + (parity & 1) * S::BYTES;
-    if constexpr (ENGINE == kPhilox) {
+    if constexpr (engine_of(ENGINE) == kPhilox) {
         ulonglong2* slots = static_cast<ulonglong2*>(smem);
         const uint64_t c_first = e0 + 3u * N + 1u;                 // counter of slot 0
         if (e0 <= ~uint64_t(0) - (3u * N + S::SLOTS)) {            // no counter of the CTA wraps
@@ -243,7 +249,7 @@ __device__ __forceinline__ void cta_event_words_pair(uint64_t key, uint64_t e0, 
     using S = WordShare<N, ENGINE, 2 * NT>;
     const int t = threadIdx.x;
     smem = static_cast<unsigned char*>(smem) + (parity & 1) * S::BYTES;
-    if constexpr (ENGINE == kPhilox) {
+    if constexpr (engine_of(ENGINE) == kPhilox) {
         ulonglong2* slots = static_cast<ulonglong2*>(smem);
         const uint64_t c_first = e0 + 3u * N + 1u;
         if (e0 <= ~uint64_t(0) - (3u * N + S::SLOTS)) {
@@ -296,7 +302,7 @@ __device__ __forceinline__ bool cta_words_pair_fill(uint64_t key, uint64_t e0, v
     using S = WordShare<N, ENGINE, 2 * NT>;
     const int t = threadIdx.x;
     smem = static_cast<unsigned char*>(smem) + (parity & 1) * S::BYTES;
-    if constexpr (ENGINE == kPhilox) {
+    if constexpr (engine_of(ENGINE) == kPhilox) {
         if (!(e0 <= ~uint64_t(0) - (3u * N + S::SLOTS))) return false;
         ulonglong2* slots = static_cast<ulonglong2*>(smem);
         const uint64_t c_first = e0 + 3u * N + 1u;
@@ -327,7 +333,7 @@ __device__ __forceinline__ void cta_words_pair_read(const void* smem, int parity
     using S = WordShare<N, ENGINE, 2 * NT>;
     const int t = threadIdx.x + h * NT;
     smem = static_cast<const unsigned char*>(smem) + (parity & 1) * S::BYTES;
-    if constexpr (ENGINE == kPhilox) {
+    if constexpr (engine_of(ENGINE) == kPhilox) {
         const ulonglong2* slots = static_cast<const ulonglong2*>(smem);
 #pragma unroll
         for (int b = 0; b < S::B; ++b) {

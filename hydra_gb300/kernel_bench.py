@@ -5,6 +5,7 @@ Channels (Philox, seed 0x3039, mother at rest):
   3    B0 -> J/psi K pi       M = 5.27934, m = (3.0969, 0.493677, 0.13957)
   4, 5 D0 -> K + 3 or 4 pi    M = 1.86484, m = (0.493677, 0.13957 x (N-1))
   6-9  six to nine pions     M = 3.0,     m = 0.13957 x N
+(--mother / --masses replace them, e.g. to time a channel that takes the float-float boosts)
   10   ten pions             M = 5.0,     m = 0.13957 x 10
 The functor of AverageOn and Evaluate is |BW(m_01)|^2 (m0 = 0.8955, G0 = 0.0473); Evaluate
 stores the generation-time weight and the functor value (16 bytes per event), Generate the
@@ -41,12 +42,20 @@ def main(argv=None):
     ap.add_argument("--precision", choices=["fp64", "fp32_fix"], default="fp32_fix")
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--mother", type=float, default=None, help="mother mass in place of the channel's")
+    ap.add_argument("--masses", default=None, help="comma-separated daughter masses in place of the channel's")
     args = ap.parse_args(argv)
     import torch
     from hydra_gb300 import api
 
     N, n = args.n_daughters, args.events
     M, masses = CHANNELS[N]
+    if args.masses:
+        masses = [float(x) for x in args.masses.split(",")]
+        if len(masses) != N:
+            ap.error("--masses needs one mass per daughter")
+    if args.mother is not None:
+        M = args.mother
     ch = api.make_channel(masses, M, 0x3039, "philox")
     fn = api.functor_bw2(0, 1, 0.8955, 0.0473)
     dev = "cuda"
@@ -84,7 +93,7 @@ def main(argv=None):
     b.record()
     torch.cuda.synchronize()
     ms = a.elapsed_time(b) / args.steps
-    line = {"op": args.op, "n_daughters": N, "events": n, "precision": args.precision, "ms": ms,
+    line = {"op": args.op, "n_daughters": N, "mother_mass": M, "events": n, "precision": args.precision, "ms": ms,
             "events_per_s": n / ms * 1e3}
     if stored:
         line["stored_gbs"] = stored / ms / 1e6
