@@ -11,8 +11,9 @@ exceed the 129 MB L2, so no flush is needed between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference] [--precision fp64]
 
---impl reference times the reference algorithm on the host cores (the oracle port of
-Hydra's cpp/omp path, all threads) on a bounded sample of the same workload.
+--impl reference times the reference itself on the host cores: Hydra's own Generate + AverageOn
+(OMP backend, all threads), built from its headers by oracle/build_ref.sh, on a bounded sample of
+the same workload (the oracle port where that build is absent).
 
 After the contract's timed loop, `parts` adds the other workloads the metric names, each timed
 once on the same GPU (skip with --no-parts):
@@ -213,27 +214,57 @@ def cpu_sample(seconds=3.0, n_sample=1 << 21, nthreads=0):
     return done / dt, cores, f"{done} events ({done // n_sample} chunks of {n_sample}), {dt:.2f} s wall"
 
 
+REF_HARNESS = REPO / "oracle" / "_ref" / "ref_harness_omp"
+
+
+def host_threads():
+    return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+
+
+def reference_cpu(n_sample, reps):
+    """The reference itself on the host cores: Hydra's PhaseSpace<5>::Generate into a Decays and
+    AverageOn(|BW|^2) through its public API, OMP backend with every host thread, built from the
+    unmodified Hydra headers by oracle/build_ref.sh (oracle/ref_harness.cpp, mode `time`).  Returns
+    (events/s of each repetition, threads), or None where the harness was not built.  The
+    reference's Generate drops the weight and stores no unweight flag, so it does less per event
+    than the GPU step it is compared with."""
+    if not REF_HARNESS.exists():
+        return None
+    threads = host_threads()
+    cmd = [str(REF_HARNESS), "time", str(N_DAUGHTERS), "0", str(SEED), str(n_sample), repr(MOTHER),
+           *map(repr, MASSES), "2", str(BW[0]), str(BW[1]), repr(BW[2]), repr(BW[3]), str(reps)]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=900, check=True,
+                       env=dict(os.environ, OMP_NUM_THREADS=str(threads)))
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    rates = [n_sample / (g + a) for g, a in zip(d["generate_all"], d["average_all"])]
+    return rates, int(d["threads"])
+
+
 def run_reference(args):
     world, rank = dist_setup(args)
     if rank != 0:
         return 0
-    rate, cores, sample = cpu_sample(seconds=max(1.0, 1.5 * args.steps / 10))
-    vals = []
-    for _ in range(args.warmup):
-        cpu_sample(seconds=0.2)
-    for _ in range(args.steps):
-        r, _, _ = cpu_sample(seconds=1.0)
-        vals.append(r)
-    value = statistics.median(vals)
+    n_sample = 1 << 22
+    ref = reference_cpu(n_sample, args.warmup + args.steps)
+    port_rate, port_cores, port_sample = cpu_sample(seconds=2.0)
+    if ref is not None:
+        rates, cores = ref
+        value = statistics.median(rates[args.warmup:])
+        kind = "reference"
+        sample = (f"per step: {n_sample} events of the workload through the reference's own Generate + "
+                  f"AverageOn (Hydra OMP backend, {cores} threads; oracle/ref_harness.cpp built by "
+                  f"oracle/build_ref.sh); median of {args.steps} steps after {args.warmup} warm-up")
+    else:
+        value, cores, kind = port_rate, port_cores, "port"
+        sample = f"{port_sample}; oracle port of Hydra's omp path (reference harness not built here)"
     n = args.n
     line = {
         "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * n / value, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded counter-based RNG)",
         "config": workload_config(n, "fp64"), "impl": "reference",
-        "cpu_baseline": {"value": value, "unit": "events/s", "cores": cores, "kind": "port",
-                         "sample": f"per step: {sample}; oracle port of Hydra's omp path (reference not "
-                                   "buildable on the GPU host: its sources are absent there)"},
+        "cpu_baseline": {"value": value, "unit": "events/s", "cores": cores, "kind": kind, "sample": sample,
+                         "port_value": port_rate, "port_sample": port_sample},
         "e2e": {"value": value, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -363,8 +394,15 @@ def run_gpu(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        rate, cores, sample = cpu_sample(seconds=3.0)
+        rate, cores, sample = cpu_sample(seconds=2.0)
         cpu = {"value": rate, "unit": "events/s", "cores": cores, "kind": "port", "sample": sample}
+        ref = reference_cpu(1 << 22, 4)
+        if ref is not None:
+            rates, rcores = ref
+            cpu = {"value": statistics.median(rates[1:]), "unit": "events/s", "cores": rcores, "kind": "reference",
+                   "sample": f"{1 << 22} events of the workload, Generate + AverageOn through the reference's own "
+                             f"API (Hydra OMP backend), median of 3 after 1 warm-up",
+                   "port_value": rate, "port_sample": sample}
 
     csum = clocks.summary()
     if rank == 0:

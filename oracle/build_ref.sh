@@ -5,9 +5,9 @@
 # fixtures, and as the timed CPU baseline of bench.py --impl reference.
 #
 # Hydra source tree: $HYDRA_SRC, else a `reference` checkout beside this
-# repository.  Where it is present, the headers ref_harness.cpp includes (the
-# list g++ -MM gives) are also staged into oracle/_ref/src/ -- a build input kept
-# out of git like the binaries -- so that the harness can be rebuilt on a machine
+# repository.  Where it is present, the headers ref_harness.cpp can reach (every
+# #include followed, oracle/stage_ref_headers.py) are also staged into
+# oracle/_ref/src/ -- a build input kept out of git like the binaries -- so that the harness can be rebuilt on a machine
 # that has the staged copy but not the source tree (the GPU host: binaries built
 # here are x86 and do not run there).  With neither, it exits 0 without building.
 #
@@ -48,13 +48,11 @@ if [ "$full" = 1 ]; then
         rm -rf "$staged"
         mkdir -p "$staged"
         for sys in CPP OMP; do
-            g++ -std=c++17 -MM -w -I"$src" "${common_defs[@]}" -DHYDRA_DEVICE_SYSTEM=$sys -fopenmp \
-                "$here/ref_harness.cpp"
-        done | tr ' \\' '\n\n' | grep "^$src/" | xargs realpath -m | sort -u | while read -r f; do
-            rel="${f#$src/}"
-            mkdir -p "$staged/$(dirname "$rel")"
-            cp "$f" "$staged/$rel"
+            g++ -std=c++17 -M -w -I"$src" "${common_defs[@]}" -DHYDRA_DEVICE_SYSTEM=$sys -fopenmp \
+                "$here/ref_harness.cpp" -MF "$staged/.deps_$sys"
         done
+        python3 "$here/stage_ref_headers.py" "$src" "$staged" "$here/ref_harness.cpp" "$staged"/.deps_*
+        rm -f "$staged"/.deps_*
         touch "$staged/.complete"
     fi
 fi

@@ -20,6 +20,8 @@
  *   hydra/detail/DenseHistogram.inl:45-103  2-D DenseHistogram::Fill(data, weights)
  *   hydra/detail/PhaseSpaceRange.inl:46-73  phase_space_range (GenerateDecay, thrust minstd_rand)
  *   hydra/detail/PhaseSpaceIntegrator.inl:37-42  PhaseSpaceIntegrator::Integrate
+ *   examples/phase_space/phsp_averaging_functor.inl, phsp_evaluating_functor.inl: wrap_lambda functors
+ *       over declarg arguments with hydra::CosHelicityAngle, through AverageOn, Evaluate, Unweight
  *
  * Usage:
  *   ref_harness rng  N engine seed n                      out.bin
@@ -27,6 +29,7 @@
  *   ref_harness avg  N engine seed n M m0..m{N-1} fsel fi fj fa fb out.bin
  *   ref_harness time N engine seed n M m0..m{N-1} fsel fi fj fa fb reps
  *   ref_harness mothers N engine seed n M m0..m{N-1} fsel fi fj fa fb out.bin
+ *   ref_harness functors 3 engine seed n M m0 m1 m2 fsel fi fj fa fb fseed out.bin
  *   ref_harness extras N engine seed n M m0..m{N-1} fsel fi fj fa fb fseed fmax g0 g1 lo0 lo1 hi0 hi1
  *                      rseed mx my mz out.bin
  * engine: 0 = hydra::philox (Philox2x64, 7 rounds), 1 = hydra::default_random_engine (squares3)
@@ -49,6 +52,7 @@
 #include <hydra/device/System.h>
 #include <hydra/detail/random/EngineR123.h>
 #include <hydra/detail/random/squares3.h>
+#include <hydra/functions/CosHelicityAngle.h>
 
 #include <array>
 #include <chrono>
@@ -59,6 +63,9 @@
 #include <utility>
 #include <vector>
 
+declarg(FJpsi, hydra::Vector4R)
+declarg(FKaon, hydra::Vector4R)
+declarg(FPion, hydra::Vector4R)
 declarg(D0, hydra::Vector4R)
 declarg(D1, hydra::Vector4R)
 declarg(D2, hydra::Vector4R)
@@ -295,6 +302,16 @@ void run_avg(Args const& a)
     write_bin(a.out, out);
 }
 
+// Threads the OMP backend uses (1 for the sequential build).
+int ref_threads()
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
 template <size_t N, typename GRND>
 void run_time(Args const& a)
 {
@@ -306,6 +323,7 @@ void run_time(Args const& a)
     auto functor = menu_lambda<N>::make(a.f);
     hydra::Decays<PT, hydra::device::sys_t> events(a.M, masses, a.n);
     double best_gen = 1e30, best_avg = 1e30;
+    std::vector<double> gen_s, avg_s;
     for (int r = 0; r < a.reps; ++r) {
         auto t0 = std::chrono::steady_clock::now();
         phsp.Generate(mother, events);
@@ -313,11 +331,21 @@ void run_time(Args const& a)
         auto s = phsp.AverageOn(hydra::device::sys, mother, functor, a.n);
         auto t2 = std::chrono::steady_clock::now();
         (void)s;
-        best_gen = std::min(best_gen, std::chrono::duration<double>(t1 - t0).count());
-        best_avg = std::min(best_avg, std::chrono::duration<double>(t2 - t1).count());
+        gen_s.push_back(std::chrono::duration<double>(t1 - t0).count());
+        avg_s.push_back(std::chrono::duration<double>(t2 - t1).count());
+        best_gen = std::min(best_gen, gen_s.back());
+        best_avg = std::min(best_avg, avg_s.back());
     }
-    std::printf("{\"n\": %zu, \"N\": %zu, \"generate_s\": %.6f, \"average_s\": %.6f}\n",
-                a.n, N, best_gen, best_avg);
+    // best times, then every repetition in order (generate_all / average_all)
+    std::printf("{\"n\": %zu, \"N\": %zu, \"generate_s\": %.6f, \"average_s\": %.6f, \"threads\": %d",
+                a.n, N, best_gen, best_avg, ref_threads());
+    for (int k = 0; k < 2; ++k) {
+        const std::vector<double>& v = k ? avg_s : gen_s;
+        std::printf(", \"%s\": [", k ? "average_all" : "generate_all");
+        for (size_t r = 0; r < v.size(); ++r) std::printf("%s%.6f", r ? ", " : "", v[r]);
+        std::printf("]");
+    }
+    std::printf("}\n");
 }
 
 // Per-event mothers for the *Mothers variants: mass M(1 + 0.05 sin(0.7 i)), momentum
@@ -464,6 +492,57 @@ void run_extras(Args const& a)
     write_bin(a.out, out);
 }
 
+// Functors written as the reference's phase-space examples write them: a wrap_lambda over
+// declarg arguments (positional conversion from the event's Vector4R tuple) calling
+// hydra::CosHelicityAngle, and two invariant masses.
+// layout: [mean, err of AverageOn(device::sys, rest, cos_theta, n)]
+//         [n rows of Evaluate(rest, (w, m13^2, m23^2, cos_theta))]
+//         [n*3*4 four-vectors after Unweight(1 + cos_theta^2 over the Decays' typed columns, -1, fseed)] [kept]
+template <size_t N, typename GRND>
+void run_functors(Args const& a)
+{
+    if constexpr (N != 3) {
+        std::fprintf(stderr, "functors mode needs N = 3\n");
+        std::exit(2);
+    } else {
+        typedef typename ptypes<N>::type PT;
+        auto phsp = make_phsp<N, GRND>(a);
+        double masses[N];
+        for (size_t i = 0; i < N; ++i) masses[i] = a.m[i];
+        hydra::Vector4R rest(a.M, 0.0, 0.0, 0.0);
+        auto cos_theta = hydra::wrap_lambda([](FJpsi j, FKaon k, FPion p) {
+            hydra::CosHelicityAngle h;
+            return h(j + k + p, k + p, k);
+        });
+        auto m13 = hydra::wrap_lambda([](FJpsi j, FKaon k, FPion p) { return (j + p).mass2(); });
+        auto m23 = hydra::wrap_lambda([](FJpsi j, FKaon k, FPion p) { return (k + p).mass2(); });
+        std::vector<double> out;
+        auto r = phsp.AverageOn(hydra::device::sys, rest, cos_theta, a.n);
+        out.push_back(r.first);
+        out.push_back(r.second);
+        hydra::multivector<hydra::tuple<double, double, double, double>, hydra::host::sys_t> data(a.n);
+        phsp.Evaluate(rest, data, m13, m23, cos_theta);
+        for (size_t i = 0; i < a.n; ++i) {
+            auto row = data[i];
+            out.push_back(hydra::get<0>(row));
+            out.push_back(hydra::get<1>(row));
+            out.push_back(hydra::get<2>(row));
+            out.push_back(hydra::get<3>(row));
+        }
+        auto u = hydra::wrap_lambda([](D0 j, D1 k, D2 p) {
+            hydra::CosHelicityAngle h;
+            const double c = h(j + k + p, k + p, k);
+            return 1.0 + c * c;
+        });
+        hydra::Decays<PT, hydra::host::sys_t> ev(a.M, masses, a.n);
+        phsp.Generate(rest, ev);
+        auto kept = ev.Unweight(u, -1.0, static_cast<size_t>(a.fseed));
+        push_events<N>(out, ev, a.n);
+        out.push_back(static_cast<double>(kept.size()));
+        write_bin(a.out, out);
+    }
+}
+
 template <size_t N, typename GRND>
 void dispatch_mode(Args const& a)
 {
@@ -473,6 +552,7 @@ void dispatch_mode(Args const& a)
     else if (a.mode == "time") run_time<N, GRND>(a);
     else if (a.mode == "mothers") run_mothers<N, GRND>(a);
     else if (a.mode == "extras") run_extras<N, GRND>(a);
+    else if (a.mode == "functors") run_functors<N, GRND>(a);
     else { std::fprintf(stderr, "unknown mode %s\n", a.mode.c_str()); std::exit(2); }
 }
 
@@ -513,6 +593,7 @@ int main(int argc, char** argv)
             a.useed = std::strtoull(argv[k++], nullptr, 0);
             for (int c = 0; c < 3; ++c) a.mom[c] = std::strtod(argv[k++], nullptr);
         }
+        if (a.mode == "functors") a.fseed = std::strtoull(argv[k++], nullptr, 0);
         if (a.mode == "extras") {
             if (argc < k + 12) { std::fprintf(stderr, "missing args\n"); return 2; }
             a.fseed = std::strtoull(argv[k++], nullptr, 0);
