@@ -1,0 +1,278 @@
+/*
+ * hps_user_kernels.cuh -- the phase-space kernels with a user functor compiled in.
+ *
+ * A functor that is not one of the C ABI's menu entries (hydra::hps_fn::One / Mass2 / BW2) cannot
+ * cross into libhps.so, so hydra::PhaseSpace::AverageOn / Evaluate and hydra::Decays::Unweight /
+ * GetEventWeights instantiate these templates in the caller's own translation unit, which must be
+ * compiled by nvcc for sm_103a.  The functor is called in device code as the reference calls it
+ * (hydra/detail/functors/AverageMother.h:272-292, EvalMother.h:285-307): on a hydra::tuple of the
+ * event's N daughters, as Vector4R; with (mother, daughters...) in the per-event-mother form; on
+ * the Decays' own column types in PhaseSpaceReweight.  The events are the library's: the same
+ * streams and, in the FP64 form, the same separately rounded operations as the reference
+ * (hydra_gb300/csrc/genbod.cuh); in the FP32_FIX form the float kinematics of genbod_f32.cuh,
+ * widened to double before the functor sees them.  The AverageOn reduction is the fixed tile tree
+ * of hps_average_on: tiles of HPS_AVG_TILE events folded with AddStatsPHSP (StatsPHSP.h:67-84)
+ * lane by lane and then across the CTA, the tile partials merged in one CTA in a fixed order, so
+ * the result does not depend on the launch shape.  Kernels defined here are templates, so that
+ * every translation unit may instantiate them.
+ */
+#ifndef HYDRA_HPS_USER_KERNELS_CUH_
+#define HYDRA_HPS_USER_KERNELS_CUH_
+
+#if !defined(__CUDACC__)
+#error "hps_user_kernels.cuh holds device code: compile this translation unit with nvcc"
+#endif
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <tuple>
+#include <type_traits>
+#include <utility>
+
+#include "../../../hydra_gb300/csrc/genbod.cuh"
+#include "../../../hydra_gb300/csrc/genbod_f32.cuh"
+#include "../../../hydra_gb300/csrc/store.cuh"
+
+namespace hydra {
+namespace detail {
+namespace user {
+
+constexpr int kThreads = 256;                          // CTA of the tile kernels
+constexpr int kPerThread = HPS_AVG_TILE / kThreads;    // events per thread and tile
+constexpr int kFinal = 1024;                           // CTA of the merges
+
+static_assert(kThreads * kPerThread == HPS_AVG_TILE, "tile shape");
+
+// The event as the reference's functors receive it: a tuple of N Vector4R.
+template <typename V, size_t N, size_t... I>
+__host__ __device__ inline auto as_tuple(const double (&p)[N][4], std::index_sequence<I...>)
+{
+    return hydra::tuple<decltype((void)I, V())...>(V(p[I][0], p[I][1], p[I][2], p[I][3])...);
+}
+
+template <typename V, size_t N>
+__host__ __device__ inline auto event_tuple(const double (&p)[N][4])
+{
+    return as_tuple<V>(p, std::make_index_sequence<N>{});
+}
+
+// The event as a tuple of given element types (each constructible from a Vector4R V): the
+// Decays' own column types, which PhaseSpaceReweight hands its functor (Decays.inl:383).
+template <typename Tup, typename V, size_t N, size_t... I>
+__host__ __device__ inline Tup as_typed_tuple(const double (&p)[N][4], std::index_sequence<I...>)
+{
+    return Tup(typename std::tuple_element<I, Tup>::type(V(p[I][0], p[I][1], p[I][2], p[I][3]))...);
+}
+
+// (mother, daughters...) for the per-event-mother form.
+template <typename V, size_t N, size_t... I>
+__host__ __device__ inline auto as_tuple_m(const double (&mo)[4], const double (&p)[N][4], std::index_sequence<I...>)
+{
+    return hydra::tuple<V, decltype((void)I, V())...>(V(mo[0], mo[1], mo[2], mo[3]),
+                                                       V(p[I][0], p[I][1], p[I][2], p[I][3])...);
+}
+
+// One event in the requested form: FP64 (the reference's arithmetic) or FP32_FIX (float
+// kinematics; ENGINE may carry hps::kPreciseForm).  p in double either way; returns the
+// generation-time weight.
+template <int N, int ENGINE, int PREC>
+__device__ __forceinline__ double event(const hps::DevChannel& ch, const hps::DevChannelF& chf, uint64_t evt,
+                                        double (&p)[N][4])
+{
+    if constexpr (PREC == HPS_PREC_FP64) {
+        return hps::f64::event<N, hps::engine_of(ENGINE)>(ch, evt, p);
+    } else {
+        uint64_t w[3 * N - 4];
+        hps::event_words<N, hps::engine_of(ENGINE)>(ch.key, evt, w);
+        float q[N][4];
+        const hps::f32::EventWeight ew = hps::f32::event_from_words<N, ENGINE>(ch, chf, w, q);
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            p[k][0] = hps::f32::widen_pos(q[k][0]);
+#pragma unroll
+            for (int c = 1; c < 4; ++c) p[k][c] = hps::f32::widen(q[k][c]);
+        }
+        return ew.weight;
+    }
+}
+
+// AverageOn (AverageMother): tile t folds events t*HPS_AVG_TILE + j + 256 k of the call, thread j
+// in order, then the CTA tree; partials[t] gets the tile's StatsPHSP.
+template <int N, int ENGINE, int PREC, typename V, typename F>
+__global__ void __launch_bounds__(kThreads)
+k_average_tiles(hps::DevChannel ch, hps::DevChannelF chf, F f, uint64_t first, uint64_t n, uint64_t ntiles,
+                hps_stats* __restrict__ partials)
+{
+    for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        hps_stats acc{0.0, 0.0, 0.0};
+        const uint64_t base = t * HPS_AVG_TILE + threadIdx.x;
+        for (int k = 0; k < kPerThread; ++k) {
+            const uint64_t e = base + (uint64_t)k * kThreads;
+            if (e < n) {
+                double p[N][4];
+                hps_stats y;
+                y.w = event<N, ENGINE, PREC>(ch, chf, first + e, p);
+                y.mean = static_cast<double>(f(event_tuple<V>(p)));
+                y.m2 = 0.0;
+                acc = hps::stats_merge(acc, y);
+            }
+        }
+        const hps_stats r = hps::block_reduce_stats<kThreads>(acc);
+        if (threadIdx.x == 0) partials[t] = r;
+    }
+}
+
+// AverageOn(mothers, functor) (AverageMothers): event e boosted by mothers[e]; the functor sees
+// (mother, daughters...).  FP64 form.
+template <int N, int ENGINE, typename V, typename F>
+__global__ void __launch_bounds__(kThreads)
+k_average_mothers_tiles(hps::DevChannel ch, F f, const double* __restrict__ mothers, uint64_t first, uint64_t n,
+                        uint64_t ntiles, hps_stats* __restrict__ partials)
+{
+    for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        hps_stats acc{0.0, 0.0, 0.0};
+        const uint64_t base = t * HPS_AVG_TILE + threadIdx.x;
+        for (int k = 0; k < kPerThread; ++k) {
+            const uint64_t e = base + (uint64_t)k * kThreads;
+            if (e < n) {
+                double mo[4];
+                for (int c = 0; c < 4; ++c) mo[c] = mothers[4 * e + c];
+                double p[N][4];
+                hps_stats y;
+                y.w = hps::f64::event_mother<N, hps::engine_of(ENGINE)>(ch, first + e, mo, p);
+                y.mean = static_cast<double>(f(as_tuple_m<V>(mo, p, std::make_index_sequence<N>{})));
+                y.m2 = 0.0;
+                acc = hps::stats_merge(acc, y);
+            }
+        }
+        const hps_stats r = hps::block_reduce_stats<kThreads>(acc);
+        if (threadIdx.x == 0) partials[t] = r;
+    }
+}
+
+// Thread j folds partials j, j + 1024, ... in order, then the fixed CTA tree.
+template <int = 0>
+__global__ void __launch_bounds__(kFinal)
+k_average_final(const hps_stats* __restrict__ partials, uint64_t ntiles, hps_stats* __restrict__ out)
+{
+    hps_stats acc{0.0, 0.0, 0.0};
+    for (uint64_t t = threadIdx.x; t < ntiles; t += kFinal) acc = hps::stats_merge(acc, partials[t]);
+    const hps_stats r = hps::block_reduce_stats<kFinal>(acc);
+    if (threadIdx.x == 0) *out = r;
+}
+
+// Evaluate (EvalMother): column 0 the generation-time weight, column k + 1 functor k.
+template <int K> struct OutColumns { double* p[K + 1]; };
+
+template <size_t I, typename V, size_t N, typename Fs>
+__device__ __forceinline__ void eval_each(const Fs& fs, const double (&p)[N][4], double* const* out, uint64_t e)
+{
+    if constexpr (I < std::tuple_size<Fs>::value) {
+        out[I + 1][e] = static_cast<double>(std::get<I>(fs)(event_tuple<V>(p)));
+        eval_each<I + 1, V>(fs, p, out, e);
+    }
+}
+
+template <int N, int ENGINE, int PREC, typename V, typename Fs, int K>
+__global__ void __launch_bounds__(kThreads)
+k_evaluate(hps::DevChannel ch, hps::DevChannelF chf, Fs fs, OutColumns<K> out, uint64_t first, uint64_t n)
+{
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < n; e += (uint64_t)gridDim.x * blockDim.x) {
+        double p[N][4];
+        const double w = event<N, ENGINE, PREC>(ch, chf, first + e, p);
+        out.p[0][e] = w;
+        eval_each<0, V>(fs, p, out.p, e);
+    }
+}
+
+// PhaseSpaceReweight (Decays.inl:372-386) on stored events: PhaseSpaceWeight recomputed from the
+// four-vectors (Decays.inl:215-231) times the functor; each CTA's largest value into block_max.
+template <int N> struct InColumns { const double* p[N]; };
+
+template <int N, typename V, typename Tup, typename F>
+__global__ void __launch_bounds__(kThreads)
+k_reweight(InColumns<N> cols, hps::DevChannel ch, F f, uint64_t n, double* __restrict__ out,
+           double* __restrict__ block_max)
+{
+    __shared__ double smax[kThreads];
+    double m = -1.0 / 0.0;
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < n; e += (uint64_t)gridDim.x * blockDim.x) {
+        double p[N][4];
+#pragma unroll
+        for (int k = 0; k < N; ++k)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) p[k][c] = cols.p[k][4 * e + c];
+        const double w = hps::f64::recomputed_weight<N>(ch.masses, ch.max_weight, p) *
+                         static_cast<double>(f(as_typed_tuple<Tup, V>(p, std::make_index_sequence<N>{})));
+        out[e] = w;
+        m = w > m ? w : m;
+    }
+    smax[threadIdx.x] = m;
+    __syncthreads();
+    for (int s = kThreads / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s && smax[threadIdx.x + s] > smax[threadIdx.x]) smax[threadIdx.x] = smax[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) block_max[blockIdx.x] = smax[0];
+}
+
+template <int = 0>
+__global__ void __launch_bounds__(kFinal)
+k_max_final(const double* __restrict__ block_max, unsigned nblocks, double* __restrict__ out)
+{
+    __shared__ double smax[kFinal];
+    double m = -1.0 / 0.0;
+    for (unsigned b = threadIdx.x; b < nblocks; b += kFinal) m = block_max[b] > m ? block_max[b] : m;
+    smax[threadIdx.x] = m;
+    __syncthreads();
+    for (int s = kFinal / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s && smax[threadIdx.x + s] > smax[threadIdx.x]) smax[threadIdx.x] = smax[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = smax[0];
+}
+
+inline unsigned grid_for(uint64_t items, unsigned threads, unsigned cap = 152u * 32u)
+{
+    const uint64_t need = (items + threads - 1) / threads;
+    return static_cast<unsigned>(need == 0 ? 1 : (need < cap ? need : cap));
+}
+
+// Host: the kernel-side channel constants of a launch.
+struct LaunchChannel {
+    hps::DevChannel ch;
+    hps::DevChannelF chf;
+    int engine;
+};
+
+inline LaunchChannel launch_channel(const hps_channel& c)
+{
+    LaunchChannel lc;
+    hps::make_channel(c, lc.ch);
+    hps::f32::make_channel_f(c, lc.chf);
+    lc.engine = c.engine == HPS_ENGINE_PHILOX ? hps::kPhilox : hps::kSquares3;
+    return lc;
+}
+
+// Calls body(std::integral_constant<int, ENGINE>) with the channel's engine, plus
+// hps::kPreciseForm where the FP32_FIX form of this N takes the float-float boosts for it.
+template <int N, typename Body>
+inline void with_engine(const LaunchChannel& lc, int precision, Body&& body)
+{
+    const bool ff = precision == HPS_PREC_FP32_FIX && N >= hps::f32::kHardMinN && N < hps::f32::kPreciseN &&
+                    lc.chf.precise != 0;
+    if (lc.engine == hps::kPhilox) {
+        if (ff) body(std::integral_constant<int, hps::kPhilox | hps::kPreciseForm>{});
+        else body(std::integral_constant<int, hps::kPhilox>{});
+    } else {
+        if (ff) body(std::integral_constant<int, hps::kSquares3 | hps::kPreciseForm>{});
+        else body(std::integral_constant<int, hps::kSquares3>{});
+    }
+}
+
+}  // namespace user
+}  // namespace detail
+}  // namespace hydra
+
+#endif  // HYDRA_HPS_USER_KERNELS_CUH_

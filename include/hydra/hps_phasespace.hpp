@@ -10,8 +10,13 @@
  * Constructors throw std::invalid_argument / std::runtime_error with the reference's messages;
  * CUDA failures throw std::system_error.
  *
- * What crosses the C ABI is the functor menu of hps.h: AverageOn / Evaluate take
- * hydra::hps_fn::One, Mass2(i, j) or BW2(i, j, mass, width) instead of an arbitrary lambda.
+ * Functors: what crosses the C ABI is the functor menu of hps.h (hydra::hps_fn::One,
+ * Mass2(i, j), BW2(i, j, mass, width)); those calls need only a C++ compiler.  Any other functor
+ * -- a hydra::wrap_lambda of a __hydra_dual__ lambda over declarg arguments, a CosHelicityAngle,
+ * a struct with a __host__ __device__ call operator -- is compiled into the kernel templates of
+ * detail/hps_user_kernels.cuh in the caller's translation unit, as the reference compiles it into
+ * its Thrust functors; such a translation unit is built with nvcc for sm_103a
+ * (--extended-lambda --expt-relaxed-constexpr, as the reference's own CUDA build).
  * hydra::Decays stores the generation-time weight beside the four-vectors (the reference
  * drops it, DecayMother.h:285); Unweight() reorders accepted events to the front.
  */
@@ -37,6 +42,31 @@
 
 #include "../hps.h"
 
+// Host/device qualifiers of the reference (hydra/detail/Config.h), empty for a host compiler.
+#if defined(__CUDACC__)
+#define HPS_HD __host__ __device__
+#ifndef __hydra_dual__
+#define __hydra_dual__ __host__ __device__
+#endif
+#ifndef __hydra_host__
+#define __hydra_host__ __host__
+#endif
+#ifndef __hydra_device__
+#define __hydra_device__ __device__
+#endif
+#else
+#define HPS_HD
+#ifndef __hydra_dual__
+#define __hydra_dual__
+#endif
+#ifndef __hydra_host__
+#define __hydra_host__
+#endif
+#ifndef __hydra_device__
+#define __hydra_device__
+#endif
+#endif
+
 namespace hydra {
 
 typedef double GReal_t;
@@ -48,27 +78,33 @@ template <typename... T> using tuple = std::tuple<T...>;
 using std::get;
 using std::make_tuple;
 
+namespace detail {
+template <typename T> struct is_std_tuple : std::false_type {};
+template <typename... T> struct is_std_tuple<std::tuple<T...>> : std::true_type {};
+template <typename T> struct always_false : std::false_type {};
+}  // namespace detail
+
 // ---------------------------------------------------------------------------------- Vector4R
 
 class Vector4R {
 public:
     Vector4R() = default;
-    Vector4R(GReal_t e, GReal_t px, GReal_t py, GReal_t pz) : v_{e, px, py, pz} {}
-    GReal_t get(GInt_t i) const { return v_[i]; }
-    void set(GInt_t i, GReal_t d) { v_[i] = d; }
-    void set(GReal_t e, GReal_t px, GReal_t py, GReal_t pz) { v_[0] = e; v_[1] = px; v_[2] = py; v_[3] = pz; }
-    GReal_t mass2() const { return v_[0] * v_[0] - v_[1] * v_[1] - v_[2] * v_[2] - v_[3] * v_[3]; }
-    GReal_t mass() const { const GReal_t m2 = mass2(); return m2 > 0.0 ? std::sqrt(m2) : 0.0; }
-    GReal_t d3mag() const { return std::sqrt(v_[1] * v_[1] + v_[2] * v_[2] + v_[3] * v_[3]); }
-    Vector4R& operator+=(const Vector4R& o) { for (int i = 0; i < 4; ++i) v_[i] += o.v_[i]; return *this; }
-    Vector4R& operator-=(const Vector4R& o) { for (int i = 0; i < 4; ++i) v_[i] -= o.v_[i]; return *this; }
-    Vector4R& operator*=(GReal_t c) { for (int i = 0; i < 4; ++i) v_[i] *= c; return *this; }
-    friend Vector4R operator+(Vector4R a, const Vector4R& b) { return a += b; }
-    friend Vector4R operator-(Vector4R a, const Vector4R& b) { return a -= b; }
-    friend Vector4R operator*(GReal_t c, Vector4R a) { return a *= c; }
-    friend Vector4R operator*(Vector4R a, GReal_t c) { return a *= c; }
+    HPS_HD Vector4R(GReal_t e, GReal_t px, GReal_t py, GReal_t pz) : v_{e, px, py, pz} {}
+    HPS_HD GReal_t get(GInt_t i) const { return v_[i]; }
+    HPS_HD void set(GInt_t i, GReal_t d) { v_[i] = d; }
+    HPS_HD void set(GReal_t e, GReal_t px, GReal_t py, GReal_t pz) { v_[0] = e; v_[1] = px; v_[2] = py; v_[3] = pz; }
+    HPS_HD GReal_t mass2() const { return v_[0] * v_[0] - v_[1] * v_[1] - v_[2] * v_[2] - v_[3] * v_[3]; }
+    HPS_HD GReal_t mass() const { const GReal_t m2 = mass2(); return m2 > 0.0 ? ::sqrt(m2) : 0.0; }
+    HPS_HD GReal_t d3mag() const { return ::sqrt(v_[1] * v_[1] + v_[2] * v_[2] + v_[3] * v_[3]); }
+    HPS_HD Vector4R& operator+=(const Vector4R& o) { for (int i = 0; i < 4; ++i) v_[i] += o.v_[i]; return *this; }
+    HPS_HD Vector4R& operator-=(const Vector4R& o) { for (int i = 0; i < 4; ++i) v_[i] -= o.v_[i]; return *this; }
+    HPS_HD Vector4R& operator*=(GReal_t c) { for (int i = 0; i < 4; ++i) v_[i] *= c; return *this; }
+    HPS_HD friend Vector4R operator+(Vector4R a, const Vector4R& b) { return a += b; }
+    HPS_HD friend Vector4R operator-(Vector4R a, const Vector4R& b) { return a -= b; }
+    HPS_HD friend Vector4R operator*(GReal_t c, Vector4R a) { return a *= c; }
+    HPS_HD friend Vector4R operator*(Vector4R a, GReal_t c) { return a *= c; }
     // Minkowski product E1 E2 - p1.p2
-    friend GReal_t operator*(const Vector4R& a, const Vector4R& b)
+    HPS_HD friend GReal_t operator*(const Vector4R& a, const Vector4R& b)
     {
         return a.v_[0] * b.v_[0] - a.v_[1] * b.v_[1] - a.v_[2] * b.v_[2] - a.v_[3] * b.v_[3];
     }
@@ -76,33 +112,77 @@ public:
     {
         return s << "(" << v.v_[0] << "," << v.v_[1] << "," << v.v_[2] << "," << v.v_[3] << ")";
     }
-    const GReal_t* data() const { return v_; }
+    HPS_HD const GReal_t* data() const { return v_; }
 
 private:
     alignas(16) GReal_t v_[4] = {0.0, 0.0, 0.0, 0.0};
 };
 
-// A named argument type, as the reference's declarg (a Vector4R or a double with a name).
+// A named argument type, as the reference's declarg (a Vector4R or a double with a name): it
+// converts from and to its value type and hands the value out through operator().
 namespace detail {
 template <typename T, bool = std::is_class<T>::value>
 struct arg_base : public T {
     arg_base() = default;
-    arg_base(T const& x) : T(x) {}
+    HPS_HD arg_base(T const& x) : T(x) {}
+    HPS_HD T& operator()() { return *this; }
+    HPS_HD T const& operator()() const { return *this; }
 };
 template <typename T>
 struct arg_base<T, false> {
     T value{};
     arg_base() = default;
-    arg_base(T x) : value(x) {}
-    operator T() const { return value; }
+    HPS_HD arg_base(T x) : value(x) {}
+    HPS_HD operator T() const { return value; }
+    HPS_HD T& operator()() { return value; }
+    HPS_HD T const& operator()() const { return value; }
 };
 }  // namespace detail
+
+// The namespace the reference's declarg puts its argument types in (code says
+// `using namespace hydra::arguments;`); the types below are declared where declarg is used.
+namespace arguments {}
 
 #define declarg(NAME, TYPE)                                              \
     struct NAME : public ::hydra::detail::arg_base<TYPE> {               \
         using ::hydra::detail::arg_base<TYPE>::arg_base;                 \
         NAME() = default;                                                \
     };
+
+// hydra::wrap_lambda (hydra/Lambda.h:528-531): a callable that takes either the lambda's own
+// arguments or one tuple whose elements convert, in order, to them -- the form in which the
+// phase-space algorithms hand an event to a functor.
+template <typename L>
+class Lambda {
+public:
+    explicit Lambda(L const& l) : fLambda(l) {}
+    template <typename... T>
+    HPS_HD auto operator()(std::tuple<T...> const& t) const
+    {
+        return call(t, std::index_sequence_for<T...>{});
+    }
+    template <typename A0, typename... T,
+              typename std::enable_if<!detail::is_std_tuple<typename std::decay<A0>::type>::value, int>::type = 0>
+    HPS_HD auto operator()(A0 const& a0, T const&... x) const
+    {
+        return fLambda(a0, x...);
+    }
+    HPS_HD L const& GetLambda() const { return fLambda; }
+
+private:
+    template <typename Tup, size_t... I>
+    HPS_HD auto call(Tup const& t, std::index_sequence<I...>) const
+    {
+        return fLambda(std::get<I>(t)...);
+    }
+    L fLambda;
+};
+
+template <typename L>
+Lambda<L> wrap_lambda(L const& l)
+{
+    return Lambda<L>(l);
+}
 
 // ----------------------------------------------------------------------------- back-ends
 
@@ -179,6 +259,20 @@ template <> struct is_menu<One> : std::true_type {};
 template <> struct is_menu<Mass2> : std::true_type {};
 template <> struct is_menu<BW2> : std::true_type {};
 }  // namespace hps_fn
+
+namespace detail {
+template <typename... F> struct all_menu : std::true_type {};
+template <typename F, typename... R>
+struct all_menu<F, R...> : std::integral_constant<bool, hps_fn::is_menu<F>::value && all_menu<R...>::value> {};
+}  // namespace detail
+
+}  // namespace hydra
+
+#if defined(__CUDACC__)
+#include "detail/hps_user_kernels.cuh"
+#endif
+
+namespace hydra {
 
 // --------------------------------------------------------------------------------- Decays
 
@@ -310,10 +404,22 @@ public:
 
     // Events | Events.GetEventWeightFunctor(functor) (Decays.h:243-250): PhaseSpaceWeight times
     // the functor, evaluated eagerly (PhaseSpaceReweight, Decays.inl:372-386).
-    template <typename Functor>
+    template <typename Functor, typename std::enable_if<!hps_fn::is_menu<Functor>::value, int>::type = 0>
     std::vector<double> GetEventWeights(Functor const& functor) const
     {
-        static_assert(hps_fn::is_menu<Functor>::value, "the functor crosses the C ABI: hydra::hps_fn::One, Mass2, BW2");
+        std::vector<double> w(fN);
+        if (!fN) return w;
+        with_device_columns([&](const double* const* cols) {
+            detail::DeviceBuffer<double> out(fN), mx(1);
+            user_reweight(cols, functor, out.p, mx.p);
+            detail::throw_cuda(cudaMemcpy(w.data(), out.p, fN * 8, cudaMemcpyDeviceToHost), "cudaMemcpy");
+        });
+        return w;
+    }
+
+    template <typename Functor, typename std::enable_if<hps_fn::is_menu<Functor>::value, int>::type = 0>
+    std::vector<double> GetEventWeights(Functor const& functor) const
+    {
         std::vector<double> w(fN);
         if (!fN) return w;
         with_device_columns([&](const double* const* cols) {
@@ -328,10 +434,30 @@ public:
     // Decays::Unweight(functor, weight, seed) (Decays.inl:458-511): hit-or-miss on
     // PhaseSpaceWeight * functor against weight, or against the largest such value when
     // weight <= 0; accepted events move to the front in their original order; returns how many.
-    template <typename Functor>
+    template <typename Functor, typename std::enable_if<!hps_fn::is_menu<Functor>::value, int>::type = 0>
     size_t Unweight(Functor const& functor, double weight = -1.0, size_t seed = 0x39abdc4529b1661cULL)
     {
-        static_assert(hps_fn::is_menu<Functor>::value, "the functor crosses the C ABI: hydra::hps_fn::One, Mass2, BW2");
+        if (!fN) return 0;
+        std::vector<uint8_t> flags(fN);
+        detail::DeviceBuffer<uint8_t> f(fN);
+        with_device_columns([&](const double* const* cols) {
+            detail::DeviceBuffer<double> rw(fN), mx(1);
+            user_reweight(cols, functor, rw.p, mx.p);
+            detail::throw_status(hps_weight_flags(fN, rw.p, weight, weight > 0.0 ? nullptr : mx.p, seed, 0, f.p,
+                                                  nullptr));
+            if (on_device) {
+                compact_device(f.p);
+                return;
+            }
+            detail::throw_cuda(cudaMemcpy(flags.data(), f.p, fN, cudaMemcpyDeviceToHost), "cudaMemcpy");
+        });
+        if (on_device) return fKept;
+        return partition_host(flags);
+    }
+
+    template <typename Functor, typename std::enable_if<hps_fn::is_menu<Functor>::value, int>::type = 0>
+    size_t Unweight(Functor const& functor, double weight = -1.0, size_t seed = 0x39abdc4529b1661cULL)
+    {
         if (!fN) return 0;
         std::vector<uint8_t> flags(fN);
         detail::DeviceBuffer<uint8_t> f(fN);
@@ -374,6 +500,35 @@ public:
     }
 
 private:
+    // PhaseSpaceWeight x functor on the stored events with the functor compiled in
+    // (detail/hps_user_kernels.cuh, nvcc only); out[i] per event, *max_dev the largest.
+    template <typename Functor>
+    void user_reweight(const double* const* cols, Functor const& functor, double* out, double* max_dev) const
+    {
+#if defined(__CUDACC__)
+        detail::user::InColumns<nparticles> in;
+        for (size_t k = 0; k < nparticles; ++k) in.p[k] = cols[k];
+        hps_channel ch{};
+        ch.n_daughters = nparticles;
+        for (size_t k = 0; k < nparticles; ++k) ch.masses[k] = fMasses[k];
+        ch.max_weight = fMaxWeight;
+        hps::DevChannel dc;
+        hps::make_channel(ch, dc);
+        const unsigned grid = detail::user::grid_for(fN, detail::user::kThreads);
+        detail::DeviceBuffer<double> bmax(grid);
+        detail::user::k_reweight<nparticles, Vector4R, value_type>
+            <<<grid, detail::user::kThreads>>>(in, dc, functor, fN, out, bmax.p);
+        detail::user::k_max_final<><<<1, detail::user::kFinal>>>(bmax.p, grid, max_dev);
+        detail::throw_cuda(cudaGetLastError(), "reweight launch");
+        detail::throw_cuda(cudaStreamSynchronize(nullptr), "cudaStreamSynchronize");
+#else
+        (void)cols; (void)functor; (void)out; (void)max_dev;
+        static_assert(detail::always_false<Functor>::value,
+                      "a functor outside the C ABI's menu (hydra::hps_fn::One, Mass2, BW2) is compiled into the "
+                      "kernels: build this translation unit with nvcc");
+#endif
+    }
+
     // stable partition of the device columns by flags (hps_unweight_compact); sets fKept
     void compact_device(const uint8_t* flags)
     {
@@ -499,6 +654,36 @@ public:
     }
     size_t size() const { return fN; }
     double* column(size_t k) { return on_device ? fDev[k].p : fHost[k].data(); }
+
+    // Row i as a tuple of the element types (copied from the device for a device multivector);
+    // prints as (c0, c1, ...), as the reference's tuples do.
+    struct row : public hydra::tuple<T...> {
+        using hydra::tuple<T...>::tuple;
+        friend std::ostream& operator<<(std::ostream& o, row const& r)
+        {
+            o << "(";
+            print(o, r, std::index_sequence_for<T...>{});
+            return o << ")";
+        }
+        template <size_t... I>
+        static void print(std::ostream& o, row const& r, std::index_sequence<I...>)
+        {
+            const double v[] = {static_cast<double>(std::get<I>(r))...};
+            for (size_t k = 0; k < sizeof...(I); ++k) o << (k ? ", " : "") << v[k];
+        }
+    };
+    row operator[](size_t i) const
+    {
+        double v[ncols];
+        for (size_t k = 0; k < ncols; ++k) {
+            if (on_device)
+                detail::throw_cuda(cudaMemcpy(&v[k], fDev[k].p + i, 8, cudaMemcpyDeviceToHost), "cudaMemcpy");
+            else
+                v[k] = fHost[k][i];
+        }
+        return make_row(v, std::index_sequence_for<T...>{});
+    }
+
     std::vector<double> GetColumn(size_t k) const
     {
         std::vector<double> out(fN);
@@ -510,6 +695,11 @@ public:
     }
 
 private:
+    template <size_t... I>
+    static row make_row(const double (&v)[ncols], std::index_sequence<I...>)
+    {
+        return row(T(v[I])...);
+    }
     size_t fN;
     detail::DeviceBuffer<double> fDev[ncols];
     std::vector<double> fHost[ncols];
@@ -552,12 +742,49 @@ public:
         }
     }
 
-    // AverageOn(policy, mother, functor, n) (PhaseSpace.inl:255-273): (mean, sqrt(M2)/W).
-    template <typename Functor, typename Policy>
+    // AverageOn(policy, mother, functor, n) (PhaseSpace.inl:255-273): (mean, sqrt(M2)/W).  A menu
+    // functor goes through hps_average_on; any other is compiled into the tile kernels of
+    // detail/hps_user_kernels.cuh (nvcc only).
+    template <typename Functor, typename Policy,
+              typename std::enable_if<!hps_fn::is_menu<Functor>::value, int>::type = 0>
     std::pair<GReal_t, GReal_t> AverageOn(Policy const&, Vector4R const& mother, Functor const& functor, size_t n)
     {
-        static_assert(hps_fn::is_menu<Functor>::value,
-                      "AverageOn across the C ABI takes hydra::hps_fn::One, Mass2 or BW2");
+#if defined(__CUDACC__)
+        hps_channel ch = channel(mother);
+        const detail::user::LaunchChannel lc = detail::user::launch_channel(ch);
+        const uint64_t ntiles = (n + HPS_AVG_TILE - 1) / HPS_AVG_TILE;
+        detail::DeviceBuffer<hps_stats> part(ntiles ? ntiles : 1), out(1);
+        const unsigned grid = static_cast<unsigned>(ntiles < 152u * 16u ? (ntiles ? ntiles : 1) : 152u * 16u);
+        const int32_t prec = fPrecision;
+        if (ntiles) {
+            detail::user::with_engine<N>(lc, prec, [&](auto E) {
+                constexpr int EE = decltype(E)::value;
+                if (prec == HPS_PREC_FP32_FIX)
+                    detail::user::k_average_tiles<N, EE, HPS_PREC_FP32_FIX, Vector4R>
+                        <<<grid, detail::user::kThreads>>>(lc.ch, lc.chf, functor, 0, n, ntiles, part.p);
+                else
+                    detail::user::k_average_tiles<N, EE, HPS_PREC_FP64, Vector4R>
+                        <<<grid, detail::user::kThreads>>>(lc.ch, lc.chf, functor, 0, n, ntiles, part.p);
+            });
+        }
+        detail::user::k_average_final<><<<1, detail::user::kFinal>>>(part.p, ntiles, out.p);
+        detail::throw_cuda(cudaGetLastError(), "AverageOn launch");
+        hps_stats s;
+        detail::throw_cuda(cudaMemcpy(&s, out.p, sizeof(s), cudaMemcpyDeviceToHost), "cudaMemcpy");
+        return std::make_pair(s.mean, std::sqrt(s.m2) / s.w);
+#else
+        (void)mother; (void)functor; (void)n;
+        static_assert(detail::always_false<Functor>::value,
+                      "a functor outside the C ABI's menu (hydra::hps_fn::One, Mass2, BW2) is compiled into the "
+                      "kernels: build this translation unit with nvcc");
+        return {};
+#endif
+    }
+
+    template <typename Functor, typename Policy,
+              typename std::enable_if<hps_fn::is_menu<Functor>::value, int>::type = 0>
+    std::pair<GReal_t, GReal_t> AverageOn(Policy const&, Vector4R const& mother, Functor const& functor, size_t n)
+    {
         hps_channel ch = channel(mother);
         detail::DeviceBuffer<hps_stats> out(1);
         detail::throw_status(hps_average_on(&ch, 0, n, &functor.f, out.p, nullptr, 0, fPrecision, nullptr));
@@ -567,11 +794,68 @@ public:
     }
 
     // Evaluate(mother, result, functors...) (PhaseSpace.inl:314-329): column 0 the weight,
-    // column k the k-th functor.
+    // column k the k-th functor.  All-menu functors go through hps_evaluate; otherwise the
+    // functors are compiled into the evaluate kernel of detail/hps_user_kernels.cuh (nvcc only).
     template <typename... T, typename Backend, typename... Functors>
     void Evaluate(Vector4R const& mother, multivector<hydra::tuple<T...>, Backend>& result, Functors const&... fs)
     {
         static_assert(sizeof...(T) == sizeof...(Functors) + 1, "one result column per functor plus the weight");
+        evaluate_impl(std::integral_constant<bool, detail::all_menu<Functors...>::value>{}, mother, result, fs...);
+    }
+
+private:
+    template <typename... T, typename Backend, typename... Functors>
+    void evaluate_impl(std::false_type, Vector4R const& mother, multivector<hydra::tuple<T...>, Backend>& result,
+                       Functors const&... fs)
+    {
+#if defined(__CUDACC__)
+        constexpr int K = sizeof...(Functors);
+        hps_channel ch = channel(mother);
+        const detail::user::LaunchChannel lc = detail::user::launch_channel(ch);
+        const size_t n = result.size();
+        const bool dev = multivector<hydra::tuple<T...>, Backend>::on_device;
+        std::vector<detail::DeviceBuffer<double>> tmp;
+        tmp.reserve(K + 1);
+        detail::user::OutColumns<K> out;
+        for (int k = 0; k <= K; ++k) {
+            if (dev) {
+                out.p[k] = result.column(k);
+            } else {
+                tmp.emplace_back(n);
+                out.p[k] = tmp.back().p;
+            }
+        }
+        const auto fns = std::make_tuple(fs...);
+        const unsigned grid = detail::user::grid_for(n, detail::user::kThreads);
+        const int32_t prec = fPrecision;
+        if (n) {
+            detail::user::with_engine<N>(lc, prec, [&](auto E) {
+                constexpr int EE = decltype(E)::value;
+                if (prec == HPS_PREC_FP32_FIX)
+                    detail::user::k_evaluate<N, EE, HPS_PREC_FP32_FIX, Vector4R>
+                        <<<grid, detail::user::kThreads>>>(lc.ch, lc.chf, fns, out, 0, n);
+                else
+                    detail::user::k_evaluate<N, EE, HPS_PREC_FP64, Vector4R>
+                        <<<grid, detail::user::kThreads>>>(lc.ch, lc.chf, fns, out, 0, n);
+            });
+            detail::throw_cuda(cudaGetLastError(), "Evaluate launch");
+        }
+        detail::throw_cuda(cudaStreamSynchronize(nullptr), "cudaStreamSynchronize");
+        if (!dev)
+            for (int k = 0; k <= K; ++k)
+                detail::throw_cuda(cudaMemcpy(result.column(k), out.p[k], n * 8, cudaMemcpyDeviceToHost), "cudaMemcpy");
+#else
+        (void)mother; (void)result;
+        static_assert(detail::always_false<hydra::tuple<Functors...>>::value,
+                      "a functor outside the C ABI's menu (hydra::hps_fn::One, Mass2, BW2) is compiled into the "
+                      "kernels: build this translation unit with nvcc");
+#endif
+    }
+
+    template <typename... T, typename Backend, typename... Functors>
+    void evaluate_impl(std::true_type, Vector4R const& mother, multivector<hydra::tuple<T...>, Backend>& result,
+                       Functors const&... fs)
+    {
         const hps_functor menu[] = {fs.f...};
         hps_channel ch = channel(mother);
         const size_t n = result.size();
@@ -593,6 +877,7 @@ public:
                 detail::throw_cuda(cudaMemcpy(result.column(k), out[k], n * 8, cudaMemcpyDeviceToHost), "cudaMemcpy");
     }
 
+public:
     // Generate(mothers, daughters) (PhaseSpace.inl:399-417, DecayMothers): event i is boosted by
     // mothers[i]; the stream, ECM and weights are those of Generate(mother, daughters).
     template <typename... P, typename Backend>
@@ -629,11 +914,45 @@ public:
 
     // AverageOn(mothers, functor) (PhaseSpace.inl:276-287, AverageMothers): the functor sees
     // (mother, daughter 0, ..., daughter N-1).
-    template <typename Functor>
+    template <typename Functor, typename std::enable_if<!hps_fn::is_menu<Functor>::value, int>::type = 0>
     std::pair<GReal_t, GReal_t> AverageOn(DaughterRange const& mothers, Functor const& functor)
     {
-        static_assert(hps_fn::is_menu<Functor>::value,
-                      "AverageOn across the C ABI takes hydra::hps_fn::One, Mass2 or BW2");
+#if defined(__CUDACC__)
+        if (fPrecision != HPS_PREC_FP64)
+            throw std::invalid_argument("[hydra::PhaseSpace]: AverageOn(mothers, functor) with a compiled-in functor "
+                                        "runs the FP64 form; SetPrecision(HPS_PREC_FP64)");
+        hps_channel ch = channel(Vector4R(fMotherMass, 0, 0, 0));
+        const detail::user::LaunchChannel lc = detail::user::launch_channel(ch);
+        detail::DeviceBuffer<double> tmo;
+        const double* mo = device_mothers(mothers, tmo);
+        const uint64_t n = mothers.n, ntiles = (n + HPS_AVG_TILE - 1) / HPS_AVG_TILE;
+        detail::DeviceBuffer<hps_stats> part(ntiles ? ntiles : 1), out(1);
+        const unsigned grid = static_cast<unsigned>(ntiles < 152u * 16u ? (ntiles ? ntiles : 1) : 152u * 16u);
+        if (ntiles) {
+            if (lc.engine == hps::kPhilox)
+                detail::user::k_average_mothers_tiles<N, hps::kPhilox, Vector4R>
+                    <<<grid, detail::user::kThreads>>>(lc.ch, functor, mo, 0, n, ntiles, part.p);
+            else
+                detail::user::k_average_mothers_tiles<N, hps::kSquares3, Vector4R>
+                    <<<grid, detail::user::kThreads>>>(lc.ch, functor, mo, 0, n, ntiles, part.p);
+        }
+        detail::user::k_average_final<><<<1, detail::user::kFinal>>>(part.p, ntiles, out.p);
+        detail::throw_cuda(cudaGetLastError(), "AverageOn launch");
+        hps_stats st;
+        detail::throw_cuda(cudaMemcpy(&st, out.p, sizeof(st), cudaMemcpyDeviceToHost), "cudaMemcpy");
+        return std::make_pair(st.mean, std::sqrt(st.m2) / st.w);
+#else
+        (void)mothers; (void)functor;
+        static_assert(detail::always_false<Functor>::value,
+                      "a functor outside the C ABI's menu (hydra::hps_fn::One, Mass2, BW2) is compiled into the "
+                      "kernels: build this translation unit with nvcc");
+        return {};
+#endif
+    }
+
+    template <typename Functor, typename std::enable_if<hps_fn::is_menu<Functor>::value, int>::type = 0>
+    std::pair<GReal_t, GReal_t> AverageOn(DaughterRange const& mothers, Functor const& functor)
+    {
         hps_channel ch = channel(Vector4R(fMotherMass, 0, 0, 0));
         detail::DeviceBuffer<double> tmo;
         const double* mo = device_mothers(mothers, tmo);

@@ -26,9 +26,10 @@ def golden_names(prefix: str = ""):
     return sorted(p.stem for p in GOLDEN.glob("*.npz") if p.stem.startswith(prefix))
 
 
-GEN_GOLDEN = [n for n in golden_names() if not n.startswith(("rng_", "avg_", "mothers_", "extras_"))]
+GEN_GOLDEN = [n for n in golden_names() if not n.startswith(("rng_", "avg_", "mothers_", "extras_", "functors_"))]
 MOTHER_GOLDEN = golden_names("mothers_")
 EXTRA_GOLDEN = golden_names("extras_")
+FUNCTOR_GOLDEN = golden_names("functors_")
 RNG_GOLDEN = golden_names("rng_")
 AVG_GOLDEN = golden_names("avg_")
 

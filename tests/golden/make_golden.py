@@ -7,7 +7,7 @@ Needs the Hydra source tree, so it runs only where that tree exists; the
 fixtures it writes are committed and read by tests/test_oracle_golden.py and
 tests/test_gpu_parity.py.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [NAME_PREFIX]
 """
 from __future__ import annotations
 
@@ -71,6 +71,15 @@ EXTRA_CASES = [
 ]
 
 
+# Functors written as the reference's phase-space examples write them (ref_harness "functors"):
+# cos(theta_K) by hydra::CosHelicityAngle inside a wrap_lambda over declarg arguments, m13^2, m23^2;
+# (name, engine, seed, n, M, masses)
+FUNCTOR_CASES = [
+    ("functors_b0_jpsikpi", 0, 0x3039, 1024, 5.27955, [3.0969, K, 0.13957061]),
+    ("functors_b0_jpsikpi_sq", 1, 777, 512, 5.27955, [3.0969, K, 0.13957061]),
+]
+
+
 def dalitz_limits(M, m):
     """Kinematic limits of (m2(p0+p1), m2(p1+p2)), the example's histogram range."""
     rest01 = sum(m[2:])
@@ -100,9 +109,27 @@ def fnum(x):
 def main():
     if not REF.exists():
         sys.exit(f"{REF} missing: run oracle/build_ref.sh first")
+    only = sys.argv[1] if len(sys.argv) > 1 else ""      # name prefix: regenerate only those
     tmp = HERE / "_tmp.bin"
     fixtures = {}
+    for name, eng, seed, n, M, m in FUNCTOR_CASES:
+        if not name.startswith(only):
+            continue
+        args = ["functors", 3, eng, seed, n, fnum(M)] + [fnum(x) for x in m] + \
+               [0, 0, 1, fnum(0.0), fnum(0.0), hex(FUNCTOR_UNWEIGHT_SEED)]
+        d = np.fromfile(run(args, tmp), dtype=np.float64)
+        rows = d[2:2 + 4 * n].reshape(n, 4)
+        o = 2 + 4 * n
+        fixtures[name] = dict(N=3, engine=eng, seed=seed, n=n, M=M, masses=np.array(m),
+                              fseed=np.uint64(FUNCTOR_UNWEIGHT_SEED), avg_mean=d[0], avg_err=d[1],
+                              eval_w=rows[:, 0].copy(), eval_m13=rows[:, 1].copy(), eval_m23=rows[:, 2].copy(),
+                              eval_cos=rows[:, 3].copy(),
+                              unw_four=d[o:o + n * 12].reshape(n, 3, 4).transpose(1, 0, 2).copy(),
+                              unw_kept=int(d[o + n * 12]))
+        assert o + n * 12 + 1 == len(d), (name, len(d))
     for name, N, eng, seed, n, M, m, f, mom in GEN_CASES:
+        if not name.startswith(only):
+            continue
         args = ["gen", N, eng, seed, n, fnum(M)] + [fnum(x) for x in m] + \
                [f[0], f[1], f[2], fnum(f[3]), fnum(f[4]), hex(UNWEIGHT_SEED)] + [fnum(x) for x in mom]
         d = np.fromfile(run(args, tmp), dtype=np.float64)
@@ -118,15 +145,21 @@ def main():
             get_seed=d[o + 4 * n + 3], n_unweighted=d[o + 4 * n + 4],
             default_seed=d[o + 4 * n + 5:o + 4 * n + 6].view(np.uint64)[0])
     for name, N, eng, seed, n in RNG_CASES:
+        if not name.startswith(only):
+            continue
         d = np.fromfile(run(["rng", N, eng, seed, n], tmp), dtype=np.uint64)
         fixtures[name] = dict(N=N, engine=eng, seed=np.uint64(seed), n=n, words=d.reshape(n, 3 * N - 4))
     for name, N, eng, seed, n, M, m, f in AVG_CASES:
+        if not name.startswith(only):
+            continue
         args = ["avg", N, eng, seed, n, fnum(M)] + [fnum(x) for x in m] + \
                [f[0], f[1], f[2], fnum(f[3]), fnum(f[4])]
         d = np.fromfile(run(args, tmp), dtype=np.float64)
         fixtures[name] = dict(N=N, engine=eng, seed=seed, n=n, M=M, masses=np.array(m),
                               functor=np.array(f), mean=d[0], err=d[1])
     for name, N, eng, seed, n, M, m, f in MOTHER_CASES:
+        if not name.startswith(only):
+            continue
         args = ["mothers", N, eng, seed, n, fnum(M)] + [fnum(x) for x in m] + \
                [f[0], f[1], f[2], fnum(f[3]), fnum(f[4])]
         d = np.fromfile(run(args, tmp), dtype=np.float64)
@@ -139,6 +172,8 @@ def main():
         fx["avg_mean"], fx["avg_err"] = d[o + 2 * n], d[o + 2 * n + 1]
         fixtures[name] = fx
     for name, N, eng, seed, n, M, m, f, fmax, grid, rseed, mom in EXTRA_CASES:
+        if not name.startswith(only):
+            continue
         if N >= 3:
             lo, hi = dalitz_limits(M, m)
         else:

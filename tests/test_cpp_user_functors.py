@@ -1,0 +1,121 @@
+"""Functors outside the C ABI's menu through the drop-in headers (include/hydra/): the functor is
+compiled by nvcc into the library's kernel templates (include/hydra/detail/hps_user_kernels.cuh),
+as the reference compiles it into its Thrust functors.
+
+* CPU: tests/cpp/phsp_user_functors.cu -- written as the reference's phase-space examples write
+  their functors (wrap_lambda over declarg arguments, hydra::CosHelicityAngle, a multivector of
+  named columns) -- compiles and links; where the reference's source tree is present (it is not
+  on a GPU host), the reference's own examples/phase_space/phsp_averaging_functor.inl and
+  phsp_evaluating_functor.inl compile against include/ with only the include path changed (their
+  TCLAP argument parser stubbed by tests/cpp/stubs/tclap/CmdLine.h).
+* GPU: the program's AverageOn / Evaluate / Unweight(functor) results against fixtures the
+  reference itself produced for the same functors (oracle/ref_harness.cpp mode "functors",
+  tests/golden/make_golden.py).
+
+Tolerances: the FP64 events are the reference's arithmetic operation for operation, but nvcc
+contracts the functors' own products into FMAs where the reference build does not, so functor
+values are compared at 1e-12 (relative for masses, absolute for cos(theta)); weights bit for
+bit; AverageOn mean / error at 1e-10 / 1e-8 of the error / relative (another reduction order);
+the events Unweight keeps and their order exactly.  FP32_FIX: 1e-6 (the precision contract of
+that form) for weights, masses to 1e-5 (m^2 differences of float four-vectors).
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from conftest import FUNCTOR_GOLDEN, REPO, load_golden
+
+SRC = REPO / "tests" / "cpp" / "phsp_user_functors.cu"
+STUBS = REPO / "tests" / "cpp" / "stubs"
+# the reference's examples, read in place where its source tree sits beside this repository
+REF_EXAMPLES = REPO.parent / "reference" / "examples" / "phase_space"
+
+
+def nvcc():
+    for c in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if c and Path(c).exists():
+            return c
+    pytest.skip("nvcc not found")
+
+
+NVCC_FLAGS = ["-std=c++17", "-O2", "-gencode", "arch=compute_103a,code=sm_103a", "--extended-lambda",
+              "--expt-relaxed-constexpr"]
+
+
+def build_program(hps, out):
+    lib_dir = str(hps.library_path().parent)
+    cmd = [nvcc(), *NVCC_FLAGS, "-I", str(REPO / "include"), str(SRC), "-L", lib_dir, "-lhps",
+           f"-Xlinker=-rpath,{lib_dir}", "-o", str(out)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return out
+
+
+def test_user_functor_program_builds(hps, tmp_path):
+    assert build_program(hps, tmp_path / "phsp_user_functors").exists()
+
+
+@pytest.mark.parametrize("example", ["phsp_averaging_functor.inl", "phsp_evaluating_functor.inl"])
+def test_reference_examples_compile_against_dropin(tmp_path, example):
+    src = REF_EXAMPLES / example
+    if not src.exists():
+        pytest.skip("the reference's source tree is not on this machine")
+    cmd = [nvcc(), "-x", "cu", *NVCC_FLAGS, "-I", str(STUBS), "-I", str(REPO / "include"), "-c", str(src),
+           "-o", str(tmp_path / "example.o")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+def run_program(exe, g, precision, out):
+    m = [repr(float(x)) for x in g["masses"]]
+    args = [str(exe), str(int(g["engine"])), str(int(g["seed"])), str(int(g["n"])), repr(float(g["M"])), *m,
+            hex(int(g["fseed"])), str(precision), str(out)]
+    r = subprocess.run(args, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    n = int(g["n"])
+    d = np.fromfile(out, dtype=np.float64)
+    rows = d[2:2 + 4 * n].reshape(n, 4)
+    o = 2 + 4 * n
+    unw = d[o:o + 12 * n].reshape(n, 3, 4).transpose(1, 0, 2)
+    return d[0], d[1], rows, unw, int(d[o + 12 * n]), r.stdout
+
+
+@pytest.fixture(scope="module")
+def program(hps, tmp_path_factory):
+    return build_program(hps, tmp_path_factory.mktemp("functors") / "phsp_user_functors")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", FUNCTOR_GOLDEN)
+def test_user_functors_fp64_match_reference(program, cuda, tmp_path, name):
+    g = load_golden(name)
+    mean, err, rows, unw, kept, stdout = run_program(program, g, 0, tmp_path / "out.bin")
+    assert stdout.startswith("<0>: (")
+    assert np.array_equal(rows[:, 0], g["eval_w"])
+    assert np.allclose(rows[:, 1], g["eval_m13"], rtol=1e-12, atol=0)
+    assert np.allclose(rows[:, 2], g["eval_m23"], rtol=1e-12, atol=0)
+    assert np.allclose(rows[:, 3], g["eval_cos"], rtol=0, atol=1e-12)
+    assert abs(mean - g["avg_mean"]) <= 1e-10 * max(abs(g["avg_mean"]), g["avg_err"])
+    assert abs(err - g["avg_err"]) <= 1e-8 * g["avg_err"]
+    assert kept == int(g["unw_kept"])
+    e4 = float((np.abs(unw - g["unw_four"]).max(axis=2) / g["unw_four"][:, :, 0]).max())
+    assert e4 <= 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", FUNCTOR_GOLDEN)
+def test_user_functors_fp32fix_within_contract(program, cuda, tmp_path, name):
+    g = load_golden(name)
+    mean, err, rows, unw, kept, _ = run_program(program, g, 1, tmp_path / "out.bin")
+    assert float((np.abs(rows[:, 0] - g["eval_w"]) / g["eval_w"]).max()) <= 1e-6
+    assert np.allclose(rows[:, 1], g["eval_m13"], rtol=1e-5, atol=0)
+    assert np.allclose(rows[:, 2], g["eval_m23"], rtol=1e-5, atol=0)
+    # the mean of cos(theta) is near 0: compare against the statistical error of the sample
+    assert abs(mean - g["avg_mean"]) <= 1e-3 * g["avg_err"]
+    assert abs(err - g["avg_err"]) <= 1e-4 * g["avg_err"]
