@@ -516,7 +516,8 @@ def batch_part(api, torch, peak, n_channels=256, check_channels=32):
     return {"workload": f"{n_channels} channels, N in 2..10, {total} events, store path (32N+8 B/event)",
             "events": total, "ms": ms, "events_per_s": total / (ms / 1e3), "gbs": gbs, "hbm_frac": gbs / peak,
             "tuning": {"ctas_per_sm": tuning[0], "store_tile_events": tuning[1],
-                       "kernel_form": ["per_N", "one_kernel"][tuning[2]], "autotune_s": tune_s},
+                       "kernel_form": ["per_N", "one_kernel"][tuning[2]], "threads_per_event": max(1, tuning[3]),
+                       "autotune_s": tune_s},
             "max_rel_err": {"four_vectors": e4, "weights": ew, "events_checked": checked,
                             "against": "FP64 form of the same events"}}
 

@@ -91,7 +91,7 @@ BATCH_ONE_KERNEL = 1     # one persistent kernel over every N
 
 class HpsBatchTuning(ctypes.Structure):
     _fields_ = [("ctas_per_sm", ctypes.c_int32), ("store_tile_events", ctypes.c_int32),
-                ("kernel_form", ctypes.c_int32)]
+                ("kernel_form", ctypes.c_int32), ("threads_per_event", ctypes.c_int32)]
 
 
 MODE_STORE, MODE_AVERAGE = 0, 1

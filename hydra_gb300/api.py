@@ -371,9 +371,12 @@ class BatchPlan:
     """Many channels in one graph launch of persistent kernels, one per N (hps_batch_*; FP32_FIX)."""
 
     def __init__(self, max_items: int, max_average_tiles: int, tuning: tuple[int, ...] | None = None):
-        """tuning: (ctas_per_sm, store_tile_events[, kernel_form]); kernel_form 0 = one kernel
-        per N (default), 1 = one kernel over every N."""
+        """tuning: (ctas_per_sm, store_tile_events[, kernel_form[, threads_per_event]]); kernel_form
+        0 = one kernel per N (default), 1 = one kernel over every N; threads_per_event 1 (default)
+        or 2 (the store items with N >= 7 computed by two threads per event)."""
         self._p = ctypes.c_void_p()
+        if tuning:
+            tuning = tuple(tuning) + (0, 1)[len(tuning) - 2:] if len(tuning) < 4 else tuple(tuning)
         t = HpsBatchTuning(*tuning) if tuning else None
         check(lib().hps_batch_create(ctypes.byref(self._p), max_items, max_average_tiles, PREC_FP32_FIX,
                                      ctypes.byref(t) if t else None))
@@ -388,20 +391,21 @@ class BatchPlan:
     def launch(self, stream=None):
         check(lib().hps_batch_launch(self._p, _stream_handle(stream)))
 
-    def tuning(self) -> tuple[int, int, int]:
+    def tuning(self) -> tuple[int, int, int, int]:
+        """(ctas_per_sm, store_tile_events, kernel_form, threads_per_event)."""
         t = HpsBatchTuning()
         check(lib().hps_batch_get_tuning(self._p, ctypes.byref(t)))
-        return t.ctas_per_sm, t.store_tile_events, t.kernel_form
+        return t.ctas_per_sm, t.store_tile_events, t.kernel_form, t.threads_per_event
 
-    def set_tuning(self, ctas_per_sm: int, store_tile_events: int, kernel_form: int = 0):
-        t = HpsBatchTuning(ctas_per_sm, store_tile_events, kernel_form)
+    def set_tuning(self, ctas_per_sm: int, store_tile_events: int, kernel_form: int = 0, threads_per_event: int = 1):
+        t = HpsBatchTuning(ctas_per_sm, store_tile_events, kernel_form, threads_per_event)
         check(lib().hps_batch_set_tuning(self._p, ctypes.byref(t)))
 
-    def autotune(self, cache_path: str | None = None, stream=None) -> tuple[int, int, int]:
+    def autotune(self, cache_path: str | None = None, stream=None) -> tuple[int, int, int, int]:
         t = HpsBatchTuning()
         check(lib().hps_batch_autotune(self._p, _stream_handle(stream),
                                        cache_path.encode() if cache_path else None, ctypes.byref(t)))
-        return t.ctas_per_sm, t.store_tile_events, t.kernel_form
+        return t.ctas_per_sm, t.store_tile_events, t.kernel_form, t.threads_per_event
 
     def close(self):
         if self._p:

@@ -58,7 +58,8 @@ def main(argv=None):
     ap.add_argument("--channels", type=int, default=256)
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--tune-cache", default=None)
-    ap.add_argument("--tuning", default=None, help="CTAS_PER_SM,STORE_TILE[,FORM] instead of autotuning")
+    ap.add_argument("--tuning", default=None,
+                    help="CTAS_PER_SM,STORE_TILE[,FORM[,THREADS_PER_EVENT]] instead of autotuning")
     args = ap.parse_args(argv)
     import torch
     from hydra_gb300 import api
@@ -117,7 +118,8 @@ def main(argv=None):
         "batched": {"ms": t_batch, "events_per_s": total / (t_batch / 1e3), "gbs": gbs,
                     "hbm_frac": (gbs / peak) if peak else None, "tuning": {"ctas_per_sm": tuning[0],
                                                                            "store_tile_events": tuning[1],
-                                                                           "kernel_form": ["per_N", "one_kernel"][tuning[2]]}},
+                                                                           "kernel_form": ["per_N", "one_kernel"][tuning[2]],
+                                                                           "threads_per_event": max(1, tuning[3])}},
         "plain_fp64_per_channel": {"ms": t_plain64, "events_per_s": total / (t_plain64 / 1e3)},
         "plain_fp32fix_per_channel": {"ms": t_plain32, "events_per_s": total / (t_plain32 / 1e3)},
         "speedup_vs_plain_fp64": t_plain64 / t_batch,

@@ -48,14 +48,19 @@ struct BatchItemDev {
 // registers than the plain form of the same N.  Each class kernel carries both engines and both
 // modes of its N; ptxas gives them 60 (N = 2) to 128 (N = 9, 10) registers, against 128 for a
 // kernel over every N.
-constexpr int kBatchClasses = 12;
+// With threads_per_event = 2, the store items of N = 7..10 go to classes 12..15 (N = c - 5),
+// whose kernels run two threads per event (store_chunk_split_f32).
+constexpr int kBatchClasses = 16;
 __host__ __device__ constexpr int class_n(int c) { return c < 9 ? c + 2 : c - 5; }
-__host__ __device__ constexpr bool class_ff(int c) { return c >= 9; }
+__host__ __device__ constexpr bool class_ff(int c) { return c >= 9 && c < 12; }
+__host__ __device__ constexpr bool class_split(int c) { return c >= 12; }
+constexpr int kSplitMinN = 7;
 inline bool ff_class_n(int N) { return N >= f32::kHardMinN && N < f32::kPreciseN; }
-inline int batch_class(int N, bool ff)
+inline int batch_class(int N, bool ff, bool split = false)
 {
     if (N < 2) return 0;
     if (N > 10) return 8;
+    if (split && N >= kSplitMinN) return N + 5;
     return (ff && ff_class_n(N)) ? N + 5 : N - 2;
 }
 // The engine field of a table entry: the engine, with kPreciseForm for the float-float classes.
@@ -71,7 +76,7 @@ struct BatchHeader {
     int32_t store_tile;
 };
 
-template <int N, int ENGINE>
+template <int N, int ENGINE, bool SPLIT = false>
 __device__ __forceinline__ void run_unit(const BatchItemDev& it, uint64_t u, int store_tile, hps_stats* partials,
                                          void* smem)
 {
@@ -80,10 +85,16 @@ __device__ __forceinline__ void run_unit(const BatchItemDev& it, uint64_t u, int
         const uint64_t hi = (lo + store_tile < it.n) ? lo + store_tile : it.n;
         // the unit fetch ends with a __syncthreads, so each unit may start at parity 0
         int parity = 0;
-        for (uint64_t cb = lo; cb < hi; cb += kTileThreads, parity ^= 1)
-            store_chunk_f32<N, ENGINE>(it.chd, it.chf, it.cols, it.weights, it.flags, it.ukey, it.first, hi, cb,
-                                       it.vec32 != 0, smem, parity);
-    } else {
+        if constexpr (SPLIT) {
+            for (uint64_t cb = lo; cb < hi; cb += kTileThreads / 2, parity ^= 1)
+                store_chunk_split_f32<N, ENGINE>(it.chd, it.chf, it.cols, it.weights, it.flags, it.ukey, it.first, hi,
+                                                 cb, it.vec32 != 0, smem, parity);
+        } else {
+            for (uint64_t cb = lo; cb < hi; cb += kTileThreads, parity ^= 1)
+                store_chunk_f32<N, ENGINE>(it.chd, it.chf, it.cols, it.weights, it.flags, it.ukey, it.first, hi, cb,
+                                           it.vec32 != 0, smem, parity);
+        }
+    } else if constexpr (!SPLIT) {
         const float K0 = *reinterpret_cast<const float*>(it.stats);      // written by k_batch_shift
         const hps_sums r = average_tile_f32<N, ENGINE>(it.chd, it.chf, it.fn, it.first, it.n, u, K0, smem);
         if (threadIdx.x == 0) reinterpret_cast<hps_sums*>(partials)[it.partial_offset + u] = r;
@@ -135,11 +146,11 @@ __device__ __forceinline__ void batch_body(const BatchItemDev* __restrict__ item
 #define HPS_UNIT(NN)                                                                             \
         case NN * 8 + 0:                                                                         \
             if constexpr (NN == class_n(CLS) && !class_ff(CLS))                                  \
-                run_unit<NN, kPhilox>(it, lu, store_tile, partials, smem);                       \
+                run_unit<NN, kPhilox, class_split(CLS)>(it, lu, store_tile, partials, smem);     \
             break;                                                                               \
         case NN * 8 + 1:                                                                         \
             if constexpr (NN == class_n(CLS) && !class_ff(CLS))                                  \
-                run_unit<NN, kSquares3>(it, lu, store_tile, partials, smem);                     \
+                run_unit<NN, kSquares3, class_split(CLS)>(it, lu, store_tile, partials, smem);   \
             break;                                                                               \
         case NN * 8 + kPreciseForm:                                                              \
             if constexpr (NN == class_n(CLS) && class_ff(CLS))                                   \
@@ -269,7 +280,9 @@ inline BatchKernel class_kernel(int c)
     static const BatchKernel k[kBatchClasses] = {k_batch_f32<0>, k_batch_f32<1>, k_batch_f32<2>,
                                                  k_batch_f32<3>, k_batch_f32<4>, k_batch_f32<5>,
                                                  k_batch_f32<6>, k_batch_f32<7>, k_batch_f32<8>,
-                                                 k_batch_f32<9>, k_batch_f32<10>, k_batch_f32<11>};
+                                                 k_batch_f32<9>, k_batch_f32<10>, k_batch_f32<11>,
+                                                 k_batch_f32<12>, k_batch_f32<13>, k_batch_f32<14>,
+                                                 k_batch_f32<15>};
     return k[c];
 }
 
@@ -283,7 +296,7 @@ struct hps_batch_plan {
     int32_t max_items = 0;
     uint64_t max_avg_tiles = 0;
     int32_t precision = HPS_PREC_FP32_FIX;
-    hps_batch_tuning tuning{16, 4096, HPS_BATCH_PER_N};   // every kernel at the CTAs that fit; short units
+    hps_batch_tuning tuning{16, 4096, HPS_BATCH_PER_N, 1};   // every kernel at the CTAs that fit; short units
     BatchItemDev* d_items = nullptr;
     BatchHeader* d_header = nullptr;
     hps_stats* d_partials = nullptr;
@@ -365,6 +378,10 @@ hps_status check_tuning(const hps_batch_tuning* t)
     if (t->kernel_form != HPS_BATCH_PER_N && t->kernel_form != HPS_BATCH_ONE_KERNEL)
         return set_error(HPS_ERR_BAD_ARG, "kernel_form %d is neither HPS_BATCH_PER_N nor HPS_BATCH_ONE_KERNEL",
                          t->kernel_form);
+    if (t->threads_per_event < 0 || t->threads_per_event > 2)       // 0 reads as 1
+        return set_error(HPS_ERR_BAD_ARG, "threads_per_event %d is neither 1 nor 2", t->threads_per_event);
+    if (t->threads_per_event == 2 && t->kernel_form != HPS_BATCH_PER_N)
+        return set_error(HPS_ERR_BAD_ARG, "threads_per_event 2 needs kernel_form HPS_BATCH_PER_N");
     return HPS_OK;
 }
 
@@ -406,8 +423,10 @@ hps_status upload_items(hps_batch_plan* p, const std::vector<hps_batch_item>& it
     // rejected below, wherever it sorts)
     std::vector<int> order(n_items);
     int32_t item_begin[kBatchClasses + 1] = {};
+    const bool split = p->tuning.threads_per_event == 2;
     auto cls = [&](int i) {
-        return batch_class(items[i].channel.n_daughters, float_float_form(&items[i].channel));
+        return batch_class(items[i].channel.n_daughters, float_float_form(&items[i].channel),
+                           split && items[i].mode == HPS_MODE_STORE);
     };
     for (int i = 0; i < n_items; ++i) ++item_begin[cls(i) + 1];
     for (int c = 0; c < kBatchClasses; ++c) item_begin[c + 1] += item_begin[c];
@@ -588,7 +607,8 @@ hps_status hps_batch_set_tuning(hps_batch_plan* p, const hps_batch_tuning* t)
     if (!p || !t) return set_error(HPS_ERR_BAD_ARG, "NULL argument");
     hps_status st = check_tuning(t);
     if (st != HPS_OK) return st;
-    const bool tile_changed = t->store_tile_events != p->tuning.store_tile_events;
+    const bool tile_changed = t->store_tile_events != p->tuning.store_tile_events ||
+                              t->threads_per_event != p->tuning.threads_per_event;
     p->tuning = *t;
     if (tile_changed && p->n_items > 0) {
         // re-cut the current items into the new store tile; done on the plan's own stream
@@ -616,7 +636,8 @@ hps_status hps_batch_autotune(hps_batch_plan* p, void* stream, const char* cache
             std::string k;
             hps_batch_tuning t;
             double ms;
-            if ((ls >> k >> t.ctas_per_sm >> t.store_tile_events >> t.kernel_form >> ms) && k == key &&
+            if ((ls >> k >> t.ctas_per_sm >> t.store_tile_events >> t.kernel_form >> t.threads_per_event >> ms) &&
+                k == key &&
                 check_tuning(&t) == HPS_OK) {
                 hps_status st = hps_batch_set_tuning(p, &t);
                 if (st == HPS_OK && chosen) *chosen = t;
@@ -630,10 +651,16 @@ hps_status hps_batch_autotune(hps_batch_plan* p, void* stream, const char* cache
     cudaEventCreate(&b);
     const int ctas[] = {1, 2, 3, 4, 6, 8};
     const int tiles[] = {4096, 16384, 65536};
+    // threads per event 2 only where there are store items it applies to (N >= 7)
+    bool any_split = false;
+    for (const hps_batch_item& it : p->items)
+        any_split = any_split || (it.mode == HPS_MODE_STORE && it.channel.n_daughters >= kSplitMinN);
     std::vector<hps_batch_tuning> cands;
     for (int form : {HPS_BATCH_PER_N, HPS_BATCH_ONE_KERNEL})
         for (int tile : tiles)
-            for (int c : ctas) cands.push_back(hps_batch_tuning{c, tile, form});
+            for (int c : ctas)
+                for (int tpe = 1; tpe <= ((any_split && form == HPS_BATCH_PER_N) ? 2 : 1); ++tpe)
+                    cands.push_back(hps_batch_tuning{c, tile, form, tpe});
     hps_batch_tuning best = p->tuning;
     float best_ms = 1e30f;
     hps_status st = HPS_OK;
@@ -658,6 +685,7 @@ hps_status hps_batch_autotune(hps_batch_plan* p, void* stream, const char* cache
         std::lock_guard<std::mutex> lock(cache_mu);
         std::ofstream outf(cache_path, std::ios::app);
         outf << key << " " << best.ctas_per_sm << " " << best.store_tile_events << " " << best.kernel_form << " "
+             << best.threads_per_event << " "
              << best_ms / 3.0f << "\n";
     }
     if (chosen) *chosen = best;

@@ -348,4 +348,43 @@ __device__ __forceinline__ void cta_words_pair_read(const void* smem, int parity
     }
 }
 
+// Two threads per event: NE consecutive events (e0 + t, t = threadIdx.x % NE) on 2 NE threads.
+// Thread k < NE + B - 1 computes slot k; every thread reads back the B items of its event.  smem
+// and parity as in cta_event_words, with WordShare<N, ENGINE, NE>.
+template <int N, int ENGINE, int NE>
+__device__ __forceinline__ void cta_event_words_split(uint64_t key, uint64_t e0, void* smem, uint64_t (&w)[3 * N - 4],
+                                                      int parity)
+{
+    using S = WordShare<N, ENGINE, NE>;
+    const int k = threadIdx.x, t = threadIdx.x % NE;
+    smem = static_cast<unsigned char*>(smem) + (parity & 1) * S::BYTES;
+    if constexpr (engine_of(ENGINE) == kPhilox) {
+        ulonglong2* slots = static_cast<ulonglong2*>(smem);
+        const uint64_t c_first = e0 + 3u * N + 1u;
+        if (e0 <= ~uint64_t(0) - (3u * N + S::SLOTS)) {
+            if (k < S::SLOTS) {
+                uint64_t o0, o1;
+                philox2x64_7(c_first + k, 0, key, o0, o1);
+                slots[k] = make_ulonglong2(o0, o1);
+            }
+            __syncthreads();
+#pragma unroll
+            for (int b = 0; b < S::B; ++b) {
+                const ulonglong2 v = slots[t + b];
+                w[2 * b] = v.x;
+                if (2 * b + 1 < S::NW) w[2 * b + 1] = v.y;
+            }
+        } else {
+            event_words<N, kPhilox>(key, e0 + t, w);
+        }
+    } else {
+        uint64_t* slots = static_cast<uint64_t*>(smem);
+        const uint64_t c_first = e0 + 3u * N;
+        if (k < S::SLOTS) slots[k] = squares3_word(key, c_first + k);
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < S::NW; ++i) w[i] = slots[t + i];
+    }
+}
+
 }  // namespace hps

@@ -106,6 +106,49 @@ __device__ __forceinline__ void store_pair_seq_f32(const DevChannel& chd, const 
     }
 }
 
+// Two threads per event: events [cb, cb + kTileThreads / 2) of the call; threads t and
+// t + kTileThreads / 2 (different warps) both compute event cb + t's stage quantities and weight,
+// and each computes and stores the daughter pairs of its half (f32::owns_pair); the first half
+// stores the weight and the flag.  The same values as store_chunk_f32, bit for bit.
+template <int N, int ENGINE, int HALF>
+__device__ __forceinline__ void store_half_f32(const DevChannel& chd, const DevChannelF& ch, const Cols& cols,
+                                               double* __restrict__ weights, uint8_t* __restrict__ flags,
+                                               uint64_t ukey, uint64_t first, uint64_t e, bool vec32,
+                                               uint64_t (&w)[3 * N - 4])
+{
+    constexpr int kForm = N >= f32::kPreciseN ? f32::kFormFull
+                          : (N >= f32::kHardMinN && (ENGINE & kPreciseForm) != 0) ? f32::kFormBoosts
+                                                                                   : f32::kFormPlain;
+    float p[N][4];
+    const f32::EventWeight ew = f32::event_body<N, ENGINE, kForm, HALF>(chd, ch, w, p);
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        if (!f32::owns_pair<HALF>(k >> 1)) continue;
+        const double v[4] = {f32::widen_pos(p[k][0]), f32::widen(p[k][1]), f32::widen(p[k][2]), f32::widen(p[k][3])};
+        store_vec4(cols.p[k], e, v, vec32);
+    }
+    if constexpr (HALF == 0) {
+        if (weights) weights[e] = ew.weight;
+        if (flags) flags[e] = f32::accept(ew, squares3_word(ukey, first + e)) ? 1 : 0;
+    }
+}
+
+template <int N, int ENGINE>
+__device__ __forceinline__ void store_chunk_split_f32(const DevChannel& chd, const DevChannelF& ch, const Cols& cols,
+                                                      double* __restrict__ weights, uint8_t* __restrict__ flags,
+                                                      uint64_t ukey, uint64_t first, uint64_t n, uint64_t cb,
+                                                      bool vec32, void* smem, int parity)
+{
+    constexpr int NE = kTileThreads / 2;
+    uint64_t w[3 * N - 4];
+    cta_event_words_split<N, ENGINE, NE>(chd.key, first + cb, smem, w, parity);
+    const uint64_t e = cb + (threadIdx.x % NE);
+    if (e < n) {
+        if (threadIdx.x < NE) store_half_f32<N, ENGINE, 0>(chd, ch, cols, weights, flags, ukey, first, e, vec32, w);
+        else store_half_f32<N, ENGINE, 1>(chd, ch, cols, weights, flags, ukey, first, e, vec32, w);
+    }
+}
+
 __device__ __forceinline__ void ff_add(float& sh, float& sl, float xh, float xl)
 {
     const float s = sh + xh;

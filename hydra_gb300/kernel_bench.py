@@ -43,6 +43,7 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--mother", type=float, default=None, help="mother mass in place of the channel's")
+    ap.add_argument("--bare", action="store_true", help="generate the Decays columns only (no weights, no flags)")
     ap.add_argument("--masses", default=None, help="comma-separated daughter masses in place of the channel's")
     args = ap.parse_args(argv)
     import torch
@@ -64,10 +65,13 @@ def main(argv=None):
         four = torch.empty((N, n, 4), dtype=torch.float64, device=dev)
         w = torch.empty(n, dtype=torch.float64, device=dev)
         fl = torch.empty(n, dtype=torch.uint8, device=dev)
-        stored = n * (32 * N + 9)
+        stored = n * (32 * N + (0 if args.bare else 9))
 
         def step():
-            api.generate(ch, 0, four, w, fl, precision=args.precision)
+            if args.bare:
+                api.generate(ch, 0, four, None, None, precision=args.precision)
+            else:
+                api.generate(ch, 0, four, w, fl, precision=args.precision)
     elif args.op == "average":
         out = torch.empty(3, dtype=torch.float64, device=dev)
         ws = torch.empty(api.average_on_workspace_size(n), dtype=torch.uint8, device=dev)

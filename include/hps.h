@@ -39,7 +39,7 @@ extern "C" {
 #endif
 
 #define HPS_MAX_DAUGHTERS 10
-#define HPS_ABI_VERSION 2
+#define HPS_ABI_VERSION 3
 
 typedef enum hps_status {
     HPS_OK = 0,
@@ -367,15 +367,20 @@ typedef struct hps_batch_item {
  * store_tile_events events (a multiple of 256), AverageOn items into tiles of HPS_AVG_TILE events.
  * kernel_form: HPS_BATCH_PER_N runs one persistent kernel per N as parallel branches of the
  * graph, each at the occupancy of its own register count; HPS_BATCH_ONE_KERNEL runs one
- * persistent kernel over every N (the register count of N = 10 for all).  Each thread owns one
- * event in both forms (its kinematics stay in that thread's registers; the random words of a
- * CTA's events are computed cooperatively).  Results do not depend on the shape. */
+ * persistent kernel over every N (the register count of N = 10 for all).  threads_per_event: 1,
+ * each thread owns one event (its kinematics stay in that thread's registers; the random words
+ * of a CTA's events are computed cooperatively); 2 (per-N form only), each store event with
+ * N >= 7 is computed by two threads of different warps, each holding half of the daughter pairs
+ * and computing the stage arithmetic and weight in full.  Results do not depend on the shape. */
 typedef enum hps_batch_form { HPS_BATCH_PER_N = 0, HPS_BATCH_ONE_KERNEL = 1 } hps_batch_form;
 
 typedef struct hps_batch_tuning {
     int32_t ctas_per_sm;
     int32_t store_tile_events;
     int32_t kernel_form;                 /* hps_batch_form */
+    int32_t threads_per_event;           /* 1 (0 reads as 1), or 2 for the store items with N >= 7: each event's
+                                            daughter pairs split between two threads (fewer
+                                            registers per thread, the stage arithmetic twice) */
 } hps_batch_tuning;
 
 typedef struct hps_batch_plan hps_batch_plan;

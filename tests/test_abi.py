@@ -36,7 +36,7 @@ def test_library_exports_every_declared_symbol(hps):
 
 
 def test_abi_version(hps):
-    assert hps.lib().hps_abi_version() == 2
+    assert hps.lib().hps_abi_version() == 3
 
 
 @pytest.mark.parametrize("name", GEN_GOLDEN)
@@ -203,10 +203,11 @@ def test_batch_tuning_checked_before_any_device_call(hps):
     """hps_batch_create validates the launch shape first (no GPU needed to see the errors)."""
     lib = hps.lib()
     plan = ctypes.c_void_p()
-    for bad, msg in [((0, 4096, 0), b"ctas_per_sm"), ((2, 1000, 0), b"store_tile_events"),
-                     ((2, 4096, 2), b"kernel_form")]:
+    for bad, msg in [((0, 4096, 0, 1), b"ctas_per_sm"), ((2, 1000, 0, 1), b"store_tile_events"),
+                     ((2, 4096, 2, 1), b"kernel_form"), ((2, 4096, 0, 3), b"threads_per_event"),
+                     ((2, 4096, 1, 2), b"needs kernel_form")]:
         t = hps.HpsBatchTuning(*bad)
         st = lib.hps_batch_create(ctypes.byref(plan), 4, 4, hps.PREC_FP32_FIX, ctypes.byref(t))
         assert st == hps.ERR_BAD_ARG
         assert msg in lib.hps_last_error()
-    assert ctypes.sizeof(hps.HpsBatchTuning) == 12
+    assert ctypes.sizeof(hps.HpsBatchTuning) == 16

@@ -120,13 +120,14 @@ def test_batch_shapes_and_autotune_do_not_change_results(api, torch, tmp_path):
             assert torch.equal(a, b)
     # the cached choice is reused
     assert plan.autotune(str(cache)) == chosen
-    # both kernel forms (one persistent kernel per N, one over every N) give the same bytes
-    for form in (0, 1):
+    # both kernel forms (one persistent kernel per N, one over every N) and two threads per event
+    # give the same bytes
+    for form, tpe in ((0, 1), (1, 1), (0, 2)):
         for r in mix:
             for t in (r[4:] if r[0] == "store" else (r[5],)):
                 t.zero_()
-        plan.set_tuning(3, 8192, form)
-        assert plan.tuning() == (3, 8192, form)
+        plan.set_tuning(3, 8192, form, tpe)
+        assert plan.tuning() == (3, 8192, form, tpe)
         plan.launch()
         torch.cuda.synchronize()
         for r, ref in zip(mix, first):
