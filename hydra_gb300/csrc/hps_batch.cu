@@ -49,7 +49,11 @@ struct BatchItemDev {
 // modes of its N; ptxas gives them 60 (N = 2) to 128 (N = 9, 10) registers, against 128 for a
 // kernel over every N.
 // With threads_per_event = 2, the store items of N = 7..10 go to classes 12..15 (N = c - 5),
-// whose kernels run two threads per event (store_chunk_split_f32).
+// whose kernels run two threads per event (store_chunk_split_f32).  Half of the daughters per
+// thread does not lower the register count much: the event's random words (3N - 4 64-bit values),
+// the stage momenta and the float-float weight are held by both threads; ptxas gives the split
+// classes 128 registers like the one-thread classes of N = 7..10, and a 3-CTA bound (80
+// registers) spills 72 to 296 bytes per thread.
 constexpr int kBatchClasses = 16;
 __host__ __device__ constexpr int class_n(int c) { return c < 9 ? c + 2 : c - 5; }
 __host__ __device__ constexpr bool class_ff(int c) { return c >= 9 && c < 12; }
@@ -174,6 +178,8 @@ k_batch_f32(const BatchItemDev* __restrict__ items, BatchHeader* __restrict__ hd
 {
     batch_body<CLS>(items, hdr, partials);
 }
+
+
 
 // The single-kernel form (hps_batch_tuning.kernel_form = HPS_BATCH_ONE_KERNEL): one persistent
 // kernel takes every unit of every N from one counter and dispatches on N, reading the item from
