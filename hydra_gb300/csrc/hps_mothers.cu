@@ -1,4 +1,4 @@
-// hps_mothers.cu -- the per-event-mother forms of Generate, AverageOn and Evaluate (FP64).
+// hps_mothers.cu -- the per-event-mother forms of Generate, AverageOn and Evaluate (FP64 and FP32_FIX).
 //
 // PhaseSpace::Generate(mothers, daughters), AverageOn(begin, end, functor) and
 // Evaluate(mothers, result, functors) (hydra/detail/PhaseSpace.inl:276-309, 331-444) use the
@@ -64,6 +64,56 @@ k_evaluate_mothers_f64(DevChannel ch, uint64_t seed, const double* __restrict__ 
         const double wt = f64::event_evalmothers<N, ENGINE>(ch, first + e, seed, mo, p);
         if (weights) weights[e] = wt;
         for (int k = 0; k < nf; ++k) out.p[k][e] = functor_with_mother<N>(fs.f[k], mo, p);
+    }
+}
+
+// FP32_FIX EvalMothers: per event, the ECM and the maximum weight of the event's own mother
+// (EvalMothers.h:143-170) in FP64, the stream hash(evt, seed) from its start, the float body with
+// the channel's float constants re-based on that ECM, and the light-cone boost into the mother's
+// frame.  The power-of-two scalings of the float-float weight products stay those of the channel's
+// nominal mother mass; they only keep the products in float range, so a mother a little heavier
+// or lighter changes nothing but the exponents.
+template <int N, int ENGINE>
+__global__ void __launch_bounds__(256)
+k_evaluate_mothers_f32fix(DevChannel ch, DevChannelF chf, uint64_t seed, const double* __restrict__ mothers,
+                          MFunctors fs, int nf, double* __restrict__ weights, MOut out, uint64_t first, uint64_t n)
+{
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < n;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        double mo[4];
+        load_mother<N>(mothers, e, mo);
+        // ECM and 1 / wtmax from the mother's mass, in the reference's order (EvalMothers.h:148-170)
+        const uint64_t evt = first + e;
+        const int32_t ievt = static_cast<int32_t>(static_cast<uint32_t>(evt));
+        DevChannel c = ch;
+        c.key = splitmix64(f64::szudzik(static_cast<uint64_t>(static_cast<int64_t>(ievt)), seed));
+        double ecm = f64::mass(mo);
+#pragma unroll
+        for (int k = 0; k < N; ++k) ecm = f64::sub(ecm, ch.masses[k]);
+        double emmax = f64::add(ecm, ch.masses[0]), emmin = 0.0, wtmax = 1.0;
+#pragma unroll
+        for (int k = 1; k < N; ++k) {
+            emmin = f64::add(emmin, ch.masses[k - 1]);
+            emmax = f64::add(emmax, ch.masses[k]);
+            wtmax = f64::mul(wtmax, f64::pdk(emmax, emmin, ch.masses[k]));
+        }
+        c.ecm = ecm;
+        c.max_weight = f64::dvd(1.0, wtmax);
+        c.boost_active = 0;
+        DevChannelF cf = chf;
+        cf.ecm = static_cast<float>(ecm);
+        cf.ecm_2m64 = cf.ecm * 0x1p-64f;
+        const double e64 = ecm * 0x1p-64;
+        cf.e64_hi = static_cast<float>(e64);
+        cf.e64_lo = static_cast<float>(e64 - static_cast<double>(cf.e64_hi));
+        uint64_t w[3 * N - 4];
+        stream_words<N, engine_of(ENGINE)>(c.key, 0, w);
+        float p[N][4];
+        const f32::EventWeight ew = f32::event_from_words<N, ENGINE>(c, cf, w, p);
+        const f32::MotherFrame mf = f32::mother_frame(mo);
+        f32::boost_to_mother<N>(p, chf.m2, mf);
+        if (weights) weights[e] = ew.weight;
+        for (int k = 0; k < nf; ++k) out.p[k][e] = f32::widen(mother_functor_f32<N>(fs.f[k], mf, p));
     }
 }
 
@@ -246,7 +296,7 @@ hps_status hps_evaluate_mothers(const hps_channel* channel, uint64_t first_evt, 
 {
     HPS_ENTRY();
     DevChannel ch;
-    hps_status st = mother_args(channel, first_evt, n, mothers, precision, &ch, false);
+    hps_status st = mother_args(channel, first_evt, n, mothers, precision, &ch, true);
     if (st != HPS_OK) return st;
     if (n_functors < 0 || n_functors > kMaxMotherFunctors)
         return set_error(HPS_ERR_BAD_ARG, "n_functors %d outside 0..%d", n_functors, kMaxMotherFunctors);
@@ -260,6 +310,16 @@ hps_status hps_evaluate_mothers(const hps_channel* channel, uint64_t first_evt, 
         oc.p[k] = out[k];
     }
     const unsigned grid = grid_for(n, 256);
+    if (precision == HPS_PREC_FP32_FIX) {
+        DevChannelF chf;
+        to_device_channel_f(channel, &chf);
+#define HPS_BODY(NN, EE)                                                                                    \
+        k_evaluate_mothers_f32fix<NN, EE><<<grid, 256, 0, as_stream(stream)>>>(ch, chf, channel->seed, mothers, fs, \
+                                                                               n_functors, weights, oc, first_evt, n);
+        HPS_DISPATCH_F32(N, channel->engine, chf.precise, HPS_BODY)
+#undef HPS_BODY
+        return cuda_status(cudaGetLastError(), "hps_evaluate_mothers launch");
+    }
 #define HPS_BODY(NN, EE)                                                                                    \
     k_evaluate_mothers_f64<NN, EE><<<grid, 256, 0, as_stream(stream)>>>(ch, channel->seed, mothers, fs, n_functors, \
                                                                          weights, oc, first_evt, n);

@@ -190,11 +190,13 @@ def test_fused_and_mothers_arguments_rejected_before_launch(hps):
     assert st == hps.ERR_BAD_ARG and b"precision" in lib.hps_last_error()
     st = lib.hps_generate_average_host(ctypes.byref(ch), 0, 10, None, None, None, 0, ctypes.byref(fn), out, 1, None)
     assert st == hps.ERR_BAD_ARG and b"host_cols" in lib.hps_last_error()
-    # EvalMothers has no FP32_FIX form; DecayMothers / AverageMothers do
+    # the mothers' forms check their precision and outputs before any launch
     mo = ctypes.c_void_p(2048)
     w = ctypes.c_void_p(4096)
     st = lib.hps_evaluate_mothers(ctypes.byref(ch), 0, 10, mo, ctypes.byref(fn), 1, w, None, 1, None)
-    assert st == hps.ERR_UNSUPPORTED and b"FP64 only" in lib.hps_last_error()
+    assert st == hps.ERR_BAD_ARG and b"output column" in lib.hps_last_error()
+    st = lib.hps_evaluate_mothers(ctypes.byref(ch), 0, 10, mo, ctypes.byref(fn), 1, w, None, 5, None)
+    assert st == hps.ERR_BAD_ARG and b"precision" in lib.hps_last_error()
     st = lib.hps_generate_mothers(ctypes.byref(ch), 0, 10, mo, None, None, 7, None)
     assert st == hps.ERR_BAD_ARG and b"precision" in lib.hps_last_error()
 
