@@ -23,6 +23,10 @@ constexpr int kAvgThreads = kTileThreads;
 // 0.191 against 0.188, N = 6 0.760 against 0.735, N = 10 2.127 against 2.080.
 __host__ __device__ constexpr bool avg_paired(int N) { return N >= 3 && N <= 5; }
 
+// Resident CTAs per SM the register allocation of the FP32_FIX tile kernels must allow (second
+// argument of __launch_bounds__; 0 leaves the choice to the compiler).
+__host__ __device__ constexpr int avg_min_ctas(int N) { return N >= 9 ? 2 : 0; }
+
 template <int N, int ENGINE>
 __global__ void __launch_bounds__(kAvgThreads)
 k_average_tiles_f64(DevChannel ch, DevFunctor fn, uint64_t first, uint64_t n, uint64_t ntiles,
@@ -83,7 +87,7 @@ k_generate_average_f64(DevChannel ch, DevFunctor fn, uint64_t first, uint64_t n,
 
 // FP32_FIX form: average_tile_f32 (tiles_f32.cuh) per tile, CTA-shared random words.
 template <int N, int ENGINE>
-__global__ void __launch_bounds__(kAvgThreads)
+__global__ void __launch_bounds__(kAvgThreads, avg_min_ctas(N))
 k_average_tiles_f32fix(DevChannel chd, DevChannelF ch, DevFunctor fn, uint64_t first, uint64_t n,
                        uint64_t ntiles, hps_stats* __restrict__ partials, const float* __restrict__ k0)
 {
@@ -97,7 +101,7 @@ k_average_tiles_f32fix(DevChannel chd, DevChannelF ch, DevFunctor fn, uint64_t f
 }
 
 template <int N, int ENGINE>
-__global__ void __launch_bounds__(kAvgThreads)
+__global__ void __launch_bounds__(kAvgThreads, avg_min_ctas(N))
 k_generate_average_f32fix(DevChannel chd, DevChannelF ch, DevFunctor fn, uint64_t first, uint64_t n,
                           uint64_t ntiles, hps_stats* __restrict__ partials, const float* __restrict__ k0,
                           StoreOut so)

@@ -41,12 +41,21 @@ k_generate_f64(DevChannel ch, Cols cols, double* __restrict__ weights, uint8_t* 
 // max_weight, the quantity FlagDaugthers tests -- against u using the generation-time weight.
 constexpr int kGenThreads = kTileThreads;
 
-// CTA size of the store kernel.  Smaller CTAs wait less at the per-chunk barrier of the shared
-// random words (at the cost of (B - 1) / NT more Philox blocks per event): at N = 5, 2^24 events,
-// 128 threads took 0.622 ms against 0.633 ms for 256 and 0.667 ms for 64.  With the float-float
-// weight (N >= 7) 256 threads are faster (N = 7: 1.31 ms against 1.39 ms; N = 10 at 2^26
-// events: 9.54 ms against 10.9 ms).
+// CTA size of the store kernel and the resident CTAs per SM its register allocation must allow
+// (the second argument of __launch_bounds__: registers are capped at 65536 / (threads x CTAs); 0
+// leaves the choice to the compiler).  Smaller CTAs wait less at the per-chunk barrier of the
+// shared random words, at the cost of (B - 1) / NT more Philox blocks per event; from N = 7 the
+// event body is long enough that 256 threads pay, and from N = 8 holding it to 80 registers (3 CTAs
+// per SM) beats the compiler's choice.  Measured at 2^24 events (ms; registers in brackets):
+//   N                  2      3      4      5      6      7      8      9      10
+//   128, compiler  0.172  0.289  0.399  0.514  0.813  1.522  1.874  2.460  2.944  (47..110)
+//   128, 1 CTA     0.168  0.298  0.411  0.539  0.858  1.516  1.901  2.449  2.827  (56..215)
+//   128, 6 CTAs    0.169  0.297  0.405  0.533  0.825  1.554  1.898  2.294  2.856  (<= 80)
+//   256, compiler  0.175  0.300  0.400  0.531  0.846  1.451  1.904  2.199  3.031  (47..142)
+//   256, 2 CTAs    0.176  0.323  0.500  0.566  0.924  1.557  1.973  2.307  2.516  (<= 128)
+//   256, 3 CTAs    0.176  0.327  0.440  0.562  0.851  1.470  1.788  2.096  2.649  (<= 80)
 __host__ __device__ constexpr int gen_threads(int N) { return N <= 6 ? 128 : kGenThreads; }
+__host__ __device__ constexpr int gen_min_ctas(int N) { return N <= 7 ? 0 : N <= 9 ? 3 : 2; }
 
 // Two events per thread and iteration (store_pair_f32: one word exchange for two chunks, and two
 // independent event bodies for the scheduler to interleave) pays where an event is short: at 2^24
@@ -75,7 +84,7 @@ __host__ __device__ constexpr int gen_events_per_iteration(int N)
 constexpr unsigned kGenMaxCtas = 152u * 128u;
 
 template <int N, int ENGINE>
-__global__ void __launch_bounds__(gen_threads(N))
+__global__ void __launch_bounds__(gen_threads(N), gen_min_ctas(N))
 k_generate_f32fix(DevChannel chd, DevChannelF ch, Cols cols, double* __restrict__ weights,
                   uint8_t* __restrict__ flags, uint64_t ukey, uint64_t first, uint64_t n, int vec32)
 {

@@ -67,12 +67,7 @@ k_evaluate_mothers_f64(DevChannel ch, uint64_t seed, const double* __restrict__ 
     }
 }
 
-// FP32_FIX EvalMothers: per event, the ECM and the maximum weight of the event's own mother
-// (EvalMothers.h:143-170) in FP64, the stream hash(evt, seed) from its start, the float body with
-// the channel's float constants re-based on that ECM, and the light-cone boost into the mother's
-// frame.  The power-of-two scalings of the float-float weight products stay those of the channel's
-// nominal mother mass; they only keep the products in float range, so a mother a little heavier
-// or lighter changes nothing but the exponents.
+// FP32_FIX EvalMothers (f32::event_evalmothers per event).
 template <int N, int ENGINE>
 __global__ void __launch_bounds__(256)
 k_evaluate_mothers_f32fix(DevChannel ch, DevChannelF chf, uint64_t seed, const double* __restrict__ mothers,
@@ -82,36 +77,9 @@ k_evaluate_mothers_f32fix(DevChannel ch, DevChannelF chf, uint64_t seed, const d
          e += (uint64_t)gridDim.x * blockDim.x) {
         double mo[4];
         load_mother<N>(mothers, e, mo);
-        // ECM and 1 / wtmax from the mother's mass, in the reference's order (EvalMothers.h:148-170)
-        const uint64_t evt = first + e;
-        const int32_t ievt = static_cast<int32_t>(static_cast<uint32_t>(evt));
-        DevChannel c = ch;
-        c.key = splitmix64(f64::szudzik(static_cast<uint64_t>(static_cast<int64_t>(ievt)), seed));
-        double ecm = f64::mass(mo);
-#pragma unroll
-        for (int k = 0; k < N; ++k) ecm = f64::sub(ecm, ch.masses[k]);
-        double emmax = f64::add(ecm, ch.masses[0]), emmin = 0.0, wtmax = 1.0;
-#pragma unroll
-        for (int k = 1; k < N; ++k) {
-            emmin = f64::add(emmin, ch.masses[k - 1]);
-            emmax = f64::add(emmax, ch.masses[k]);
-            wtmax = f64::mul(wtmax, f64::pdk(emmax, emmin, ch.masses[k]));
-        }
-        c.ecm = ecm;
-        c.max_weight = f64::dvd(1.0, wtmax);
-        c.boost_active = 0;
-        DevChannelF cf = chf;
-        cf.ecm = static_cast<float>(ecm);
-        cf.ecm_2m64 = cf.ecm * 0x1p-64f;
-        const double e64 = ecm * 0x1p-64;
-        cf.e64_hi = static_cast<float>(e64);
-        cf.e64_lo = static_cast<float>(e64 - static_cast<double>(cf.e64_hi));
-        uint64_t w[3 * N - 4];
-        stream_words<N, engine_of(ENGINE)>(c.key, 0, w);
         float p[N][4];
-        const f32::EventWeight ew = f32::event_from_words<N, ENGINE>(c, cf, w, p);
-        const f32::MotherFrame mf = f32::mother_frame(mo);
-        f32::boost_to_mother<N>(p, chf.m2, mf);
+        f32::MotherFrame mf;
+        const f32::EventWeight ew = f32::event_evalmothers<N, ENGINE>(ch, chf, first + e, seed, mo, p, mf);
         if (weights) weights[e] = ew.weight;
         for (int k = 0; k < nf; ++k) out.p[k][e] = f32::widen(mother_functor_f32<N>(fs.f[k], mf, p));
     }

@@ -37,11 +37,18 @@ __device__ __forceinline__ void store_event_f32(const float (&p)[N][4], const f3
                                                 uint8_t* __restrict__ flags, uint64_t ukey, uint64_t first,
                                                 uint64_t e, bool vec32)
 {
+    // the alignment test is uniform: one branch around all N stores, not one per store
+    if (vec32) {
 #pragma unroll
-    for (int k = 0; k < N; ++k) {
-        const double v[4] = {f32::widen_pos(p[k][0]), f32::widen(p[k][1]), f32::widen(p[k][2]),
-                             f32::widen(p[k][3])};
-        store_vec4(cols.p[k], e, v, vec32);
+        for (int k = 0; k < N; ++k)
+            st_v4_f64(cols.p[k] + 4 * e, f32::widen_pos(p[k][0]), f32::widen(p[k][1]), f32::widen(p[k][2]),
+                      f32::widen(p[k][3]));
+    } else {
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            st_v2_f64(cols.p[k] + 4 * e, f32::widen_pos(p[k][0]), f32::widen(p[k][1]));
+            st_v2_f64(cols.p[k] + 4 * e + 2, f32::widen(p[k][2]), f32::widen(p[k][3]));
+        }
     }
     if (weights) weights[e] = ew.weight;
     if (flags) flags[e] = f32::accept(ew, squares3_word(ukey, first + e)) ? 1 : 0;

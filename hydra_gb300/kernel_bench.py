@@ -37,7 +37,7 @@ CHANNELS = {
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--op", choices=["generate", "average", "evaluate"], default="evaluate")
-    ap.add_argument("--n-daughters", type=int, choices=sorted(CHANNELS), default=5)
+    ap.add_argument("--n-daughters", default="5", help="N, or a comma-separated list of N (one line each)")
     ap.add_argument("--events", type=int, default=1 << 24)
     ap.add_argument("--precision", choices=["fp64", "fp32_fix"], default="fp32_fix")
     ap.add_argument("--steps", type=int, default=10)
@@ -46,10 +46,19 @@ def main(argv=None):
     ap.add_argument("--bare", action="store_true", help="generate the Decays columns only (no weights, no flags)")
     ap.add_argument("--masses", default=None, help="comma-separated daughter masses in place of the channel's")
     args = ap.parse_args(argv)
+    ns = [int(x) for x in args.n_daughters.split(",")]
+    if any(N not in CHANNELS for N in ns):
+        ap.error(f"--n-daughters takes values in {sorted(CHANNELS)}")
+    for N in ns:
+        run(ap, args, N)
+    return 0
+
+
+def run(ap, args, N):
     import torch
     from hydra_gb300 import api
 
-    N, n = args.n_daughters, args.events
+    n = args.events
     M, masses = CHANNELS[N]
     if args.masses:
         masses = [float(x) for x in args.masses.split(",")]
@@ -102,7 +111,6 @@ def main(argv=None):
     if stored:
         line["stored_gbs"] = stored / ms / 1e6
     print(json.dumps(line), flush=True)
-    return 0
 
 
 if __name__ == "__main__":

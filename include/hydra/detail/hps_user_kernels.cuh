@@ -123,12 +123,37 @@ k_average_tiles(hps::DevChannel ch, hps::DevChannelF chf, F f, uint64_t first, u
     }
 }
 
+// One event of the per-event-mother form (AverageMothers.h:134-285): generated at the channel's
+// ECM and boosted into the frame of its mother mo.  FP64: the reference's arithmetic; FP32_FIX:
+// the float event of genbod_f32.cuh with the light-cone boost into the mother's frame, widened.
+template <int N, int ENGINE, int PREC>
+__device__ __forceinline__ double event_mother(const hps::DevChannel& ch, const hps::DevChannelF& chf, uint64_t evt,
+                                               const double (&mo)[4], double (&p)[N][4])
+{
+    if constexpr (PREC == HPS_PREC_FP64) {
+        return hps::f64::event_mother<N, hps::engine_of(ENGINE)>(ch, evt, mo, p);
+    } else {
+        uint64_t w[3 * N - 4];
+        hps::event_words<N, hps::engine_of(ENGINE)>(ch.key, evt, w);
+        float q[N][4];
+        const hps::f32::EventWeight ew = hps::f32::event_from_words<N, ENGINE>(ch, chf, w, q);
+        hps::f32::boost_to_mother<N>(q, chf.m2, hps::f32::mother_frame(mo));
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            p[k][0] = hps::f32::widen_pos(q[k][0]);
+#pragma unroll
+            for (int c = 1; c < 4; ++c) p[k][c] = hps::f32::widen(q[k][c]);
+        }
+        return ew.weight;
+    }
+}
+
 // AverageOn(mothers, functor) (AverageMothers): event e boosted by mothers[e]; the functor sees
-// (mother, daughters...).  FP64 form.
-template <int N, int ENGINE, typename V, typename F>
+// (mother, daughters...).
+template <int N, int ENGINE, int PREC, typename V, typename F>
 __global__ void __launch_bounds__(kThreads)
-k_average_mothers_tiles(hps::DevChannel ch, F f, const double* __restrict__ mothers, uint64_t first, uint64_t n,
-                        uint64_t ntiles, hps_stats* __restrict__ partials)
+k_average_mothers_tiles(hps::DevChannel ch, hps::DevChannelF chf, F f, const double* __restrict__ mothers,
+                        uint64_t first, uint64_t n, uint64_t ntiles, hps_stats* __restrict__ partials)
 {
     for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         hps_stats acc{0.0, 0.0, 0.0};
@@ -140,7 +165,7 @@ k_average_mothers_tiles(hps::DevChannel ch, F f, const double* __restrict__ moth
                 for (int c = 0; c < 4; ++c) mo[c] = mothers[4 * e + c];
                 double p[N][4];
                 hps_stats y;
-                y.w = hps::f64::event_mother<N, hps::engine_of(ENGINE)>(ch, first + e, mo, p);
+                y.w = event_mother<N, ENGINE, PREC>(ch, chf, first + e, mo, p);
                 y.mean = static_cast<double>(f(as_tuple_m<V>(mo, p, std::make_index_sequence<N>{})));
                 y.m2 = 0.0;
                 acc = hps::stats_merge(acc, y);
@@ -183,6 +208,47 @@ k_evaluate(hps::DevChannel ch, hps::DevChannelF chf, Fs fs, OutColumns<K> out, u
         const double w = event<N, ENGINE, PREC>(ch, chf, first + e, p);
         out.p[0][e] = w;
         eval_each<0, V>(fs, p, out.p, e);
+    }
+}
+
+// Evaluate(mothers, result, functors...) (EvalMothers.h:143-305): the stream hash((int)evt, seed)
+// per event, ECM and maximum weight from the event's own mother, the daughters boosted into its
+// frame; column 0 the weight, column k + 1 functor k on (mother, daughters...).
+template <size_t I, typename V, size_t N, typename Fs>
+__device__ __forceinline__ void eval_each_m(const Fs& fs, const double (&mo)[4], const double (&p)[N][4],
+                                            double* const* out, uint64_t e)
+{
+    if constexpr (I < std::tuple_size<Fs>::value) {
+        out[I + 1][e] = static_cast<double>(std::get<I>(fs)(as_tuple_m<V>(mo, p, std::make_index_sequence<N>{})));
+        eval_each_m<I + 1, V>(fs, mo, p, out, e);
+    }
+}
+
+template <int N, int ENGINE, int PREC, typename V, typename Fs, int K>
+__global__ void __launch_bounds__(kThreads)
+k_evaluate_mothers(hps::DevChannel ch, hps::DevChannelF chf, uint64_t seed, const double* __restrict__ mothers,
+                   Fs fs, OutColumns<K> out, uint64_t first, uint64_t n)
+{
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < n; e += (uint64_t)gridDim.x * blockDim.x) {
+        double mo[4];
+        for (int c = 0; c < 4; ++c) mo[c] = mothers[4 * e + c];
+        double p[N][4];
+        double w;
+        if constexpr (PREC == HPS_PREC_FP64) {
+            w = hps::f64::event_evalmothers<N, hps::engine_of(ENGINE)>(ch, first + e, seed, mo, p);
+        } else {
+            float q[N][4];
+            hps::f32::MotherFrame mf;
+            w = hps::f32::event_evalmothers<N, ENGINE>(ch, chf, first + e, seed, mo, q, mf).weight;
+#pragma unroll
+            for (int k = 0; k < N; ++k) {
+                p[k][0] = hps::f32::widen_pos(q[k][0]);
+#pragma unroll
+                for (int c = 1; c < 4; ++c) p[k][c] = hps::f32::widen(q[k][c]);
+            }
+        }
+        out.p[0][e] = w;
+        eval_each_m<0, V>(fs, mo, p, out.p, e);
     }
 }
 

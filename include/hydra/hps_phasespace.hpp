@@ -918,9 +918,6 @@ public:
     std::pair<GReal_t, GReal_t> AverageOn(DaughterRange const& mothers, Functor const& functor)
     {
 #if defined(__CUDACC__)
-        if (fPrecision != HPS_PREC_FP64)
-            throw std::invalid_argument("[hydra::PhaseSpace]: AverageOn(mothers, functor) with a compiled-in functor "
-                                        "runs the FP64 form; SetPrecision(HPS_PREC_FP64)");
         hps_channel ch = channel(Vector4R(fMotherMass, 0, 0, 0));
         const detail::user::LaunchChannel lc = detail::user::launch_channel(ch);
         detail::DeviceBuffer<double> tmo;
@@ -928,13 +925,17 @@ public:
         const uint64_t n = mothers.n, ntiles = (n + HPS_AVG_TILE - 1) / HPS_AVG_TILE;
         detail::DeviceBuffer<hps_stats> part(ntiles ? ntiles : 1), out(1);
         const unsigned grid = static_cast<unsigned>(ntiles < 152u * 16u ? (ntiles ? ntiles : 1) : 152u * 16u);
+        const int32_t prec = fPrecision;
         if (ntiles) {
-            if (lc.engine == hps::kPhilox)
-                detail::user::k_average_mothers_tiles<N, hps::kPhilox, Vector4R>
-                    <<<grid, detail::user::kThreads>>>(lc.ch, functor, mo, 0, n, ntiles, part.p);
-            else
-                detail::user::k_average_mothers_tiles<N, hps::kSquares3, Vector4R>
-                    <<<grid, detail::user::kThreads>>>(lc.ch, functor, mo, 0, n, ntiles, part.p);
+            detail::user::with_engine<N>(lc, prec, [&](auto E) {
+                constexpr int EE = decltype(E)::value;
+                if (prec == HPS_PREC_FP32_FIX)
+                    detail::user::k_average_mothers_tiles<N, EE, HPS_PREC_FP32_FIX, Vector4R>
+                        <<<grid, detail::user::kThreads>>>(lc.ch, lc.chf, functor, mo, 0, n, ntiles, part.p);
+                else
+                    detail::user::k_average_mothers_tiles<N, EE, HPS_PREC_FP64, Vector4R>
+                        <<<grid, detail::user::kThreads>>>(lc.ch, lc.chf, functor, mo, 0, n, ntiles, part.p);
+            });
         }
         detail::user::k_average_final<><<<1, detail::user::kFinal>>>(part.p, ntiles, out.p);
         detail::throw_cuda(cudaGetLastError(), "AverageOn launch");
@@ -965,11 +966,72 @@ public:
     }
 
     // Evaluate(mothers, result, functors...) (PhaseSpace.inl:334-348, EvalMothers): its own stream
-    // per event (hash(event, seed)), ECM and maximum weight from each mother's mass; FP64 only.
+    // per event (hash(event, seed)), ECM and maximum weight from each mother's mass; the functors
+    // see (mother, daughters...).  All-menu functors go through hps_evaluate_mothers; otherwise they
+    // are compiled into the kernel of detail/hps_user_kernels.cuh (nvcc only).
     template <typename... T, typename Backend, typename... Functors>
     void Evaluate(DaughterRange const& mothers, multivector<hydra::tuple<T...>, Backend>& result, Functors const&... fs)
     {
         static_assert(sizeof...(T) == sizeof...(Functors) + 1, "one result column per functor plus the weight");
+        evaluate_mothers_impl(std::integral_constant<bool, detail::all_menu<Functors...>::value>{}, mothers, result,
+                              fs...);
+    }
+
+private:
+    template <typename... T, typename Backend, typename... Functors>
+    void evaluate_mothers_impl(std::false_type, DaughterRange const& mothers,
+                               multivector<hydra::tuple<T...>, Backend>& result, Functors const&... fs)
+    {
+#if defined(__CUDACC__)
+        constexpr int K = sizeof...(Functors);
+        hps_channel ch = channel(Vector4R(fMotherMass, 0, 0, 0));
+        const detail::user::LaunchChannel lc = detail::user::launch_channel(ch);
+        detail::DeviceBuffer<double> tmo;
+        const double* mo = device_mothers(mothers, tmo);
+        const size_t n = mothers.n;
+        const bool dev = multivector<hydra::tuple<T...>, Backend>::on_device;
+        std::vector<detail::DeviceBuffer<double>> tmp;
+        tmp.reserve(K + 1);
+        detail::user::OutColumns<K> out;
+        for (int k = 0; k <= K; ++k) {
+            if (dev) {
+                out.p[k] = result.column(k);
+            } else {
+                tmp.emplace_back(n);
+                out.p[k] = tmp.back().p;
+            }
+        }
+        const auto fns = std::make_tuple(fs...);
+        const unsigned grid = detail::user::grid_for(n, detail::user::kThreads);
+        const int32_t prec = fPrecision;
+        if (n) {
+            detail::user::with_engine<N>(lc, prec, [&](auto E) {
+                constexpr int EE = decltype(E)::value;
+                if (prec == HPS_PREC_FP32_FIX)
+                    detail::user::k_evaluate_mothers<N, EE, HPS_PREC_FP32_FIX, Vector4R>
+                        <<<grid, detail::user::kThreads>>>(lc.ch, lc.chf, ch.seed, mo, fns, out, 0, n);
+                else
+                    detail::user::k_evaluate_mothers<N, EE, HPS_PREC_FP64, Vector4R>
+                        <<<grid, detail::user::kThreads>>>(lc.ch, lc.chf, ch.seed, mo, fns, out, 0, n);
+            });
+            detail::throw_cuda(cudaGetLastError(), "Evaluate launch");
+        }
+        detail::throw_cuda(cudaStreamSynchronize(nullptr), "cudaStreamSynchronize");
+        if (!dev)
+            for (int k = 0; k <= K; ++k)
+                detail::throw_cuda(cudaMemcpy(result.column(k), out.p[k], n * 8, cudaMemcpyDeviceToHost), "cudaMemcpy");
+#else
+        (void)mothers; (void)result;
+        static_assert(detail::always_false<hydra::tuple<Functors...>>::value,
+                      "a functor outside the C ABI's menu (hydra::hps_fn::One, Mass2, BW2) is compiled into the "
+                      "kernels: build this translation unit with nvcc");
+#endif
+    }
+
+    template <typename... T, typename Backend, typename... Functors>
+    void evaluate_mothers_impl(std::true_type, DaughterRange const& mothers,
+                               multivector<hydra::tuple<T...>, Backend>& result, Functors const&... fs)
+    {
         const hps_functor menu[] = {fs.f...};
         hps_channel ch = channel(Vector4R(fMotherMass, 0, 0, 0));
         detail::DeviceBuffer<double> tmo;
@@ -987,13 +1049,14 @@ public:
             }
         }
         detail::throw_status(hps_evaluate_mothers(&ch, 0, n, mo, menu, sizeof...(Functors), out[0], out + 1,
-                                                  HPS_PREC_FP64, nullptr));
+                                                  fPrecision, nullptr));
         detail::throw_cuda(cudaStreamSynchronize(nullptr), "cudaStreamSynchronize");
         if (!dev)
             for (size_t k = 0; k <= sizeof...(Functors); ++k)
                 detail::throw_cuda(cudaMemcpy(result.column(k), out[k], n * 8, cudaMemcpyDeviceToHost), "cudaMemcpy");
     }
 
+public:
     GInt_t GetSeed() const { return static_cast<GInt_t>(fSeed); }
     void SetSeed(GInt_t seed) { fSeed = static_cast<size_t>(static_cast<long long>(seed)); }
     const GReal_t* GetMasses() const { return fMasses; }

@@ -120,5 +120,11 @@ def test_chain_example_matches_oracle(hps, cuda, oracle, tmp_path, precision, to
     rmean, rm2, rW = oracle.average_mothers(och, oracle.make_functor(1, 1, 2), 0, jpsi)
     assert abs(d["avg_mean"] - rmean) <= max(tol, 1e-10) * abs(rmean)
     rw, rf, _ = oracle.evaluate_mothers(och, oracle.make_functor(1, 0, 1), 0, jpsi)
-    assert np.array_equal(np.array(d["eval_w"]), rw)
-    np.testing.assert_allclose(d["eval_f"], rf, rtol=1e-12, atol=0)
+    if precision == 0:
+        assert np.array_equal(np.array(d["eval_w"]), rw)
+        np.testing.assert_allclose(d["eval_f"], rf, rtol=1e-12, atol=0)
+    else:
+        # FP32_FIX EvalMothers: weights within the form's 1e-6; m^2(J/psi + mu+) from a muon that is
+        # within 1e-6 x the J/psi's gamma (about 1.14) of the oracle's
+        np.testing.assert_allclose(d["eval_w"], rw, rtol=1e-6, atol=0)
+        np.testing.assert_allclose(d["eval_f"], rf, rtol=2e-6, atol=0)

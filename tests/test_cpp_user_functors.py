@@ -32,6 +32,7 @@ import pytest
 from conftest import FUNCTOR_GOLDEN, REPO, load_golden
 
 SRC = REPO / "tests" / "cpp" / "phsp_user_functors.cu"
+SRC_MOTHERS = REPO / "tests" / "cpp" / "phsp_user_mothers.cu"
 STUBS = REPO / "tests" / "cpp" / "stubs"
 # the reference's examples, read in place where its source tree sits beside this repository
 REF_EXAMPLES = REPO.parent / "reference" / "examples" / "phase_space"
@@ -48,9 +49,9 @@ NVCC_FLAGS = ["-std=c++17", "-O2", "-gencode", "arch=compute_103a,code=sm_103a",
               "--expt-relaxed-constexpr"]
 
 
-def build_program(hps, out):
+def build_program(hps, out, src=SRC):
     lib_dir = str(hps.library_path().parent)
-    cmd = [nvcc(), *NVCC_FLAGS, "-I", str(REPO / "include"), str(SRC), "-L", lib_dir, "-lhps",
+    cmd = [nvcc(), *NVCC_FLAGS, "-I", str(REPO / "include"), str(src), "-L", lib_dir, "-lhps",
            f"-Xlinker=-rpath,{lib_dir}", "-o", str(out)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
@@ -59,6 +60,10 @@ def build_program(hps, out):
 
 def test_user_functor_program_builds(hps, tmp_path):
     assert build_program(hps, tmp_path / "phsp_user_functors").exists()
+
+
+def test_user_functor_mothers_program_builds(hps, tmp_path):
+    assert build_program(hps, tmp_path / "phsp_user_mothers", SRC_MOTHERS).exists()
 
 
 @pytest.mark.parametrize("example", ["phsp_averaging_functor.inl", "phsp_evaluating_functor.inl"])
@@ -119,3 +124,45 @@ def test_user_functors_fp32fix_within_contract(program, cuda, tmp_path, name):
     # the mean of cos(theta) is near 0: compare against the statistical error of the sample
     assert abs(mean - g["avg_mean"]) <= 1e-3 * g["avg_err"]
     assert abs(err - g["avg_err"]) <= 1e-4 * g["avg_err"]
+
+
+@pytest.fixture(scope="module")
+def mothers_program(hps, tmp_path_factory):
+    return build_program(hps, tmp_path_factory.mktemp("mothers") / "phsp_user_mothers", SRC_MOTHERS)
+
+
+def run_mothers(exe, n, precision):
+    import json
+    r = subprocess.run([str(exe), str(n), str(precision)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    d = json.loads(r.stdout)
+    return {k: np.asarray(v) for k, v in d.items()}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32_fix"])
+def test_user_functor_with_mothers_matches_menu(mothers_program, cuda, precision):
+    """AverageOn(mothers, F) and Evaluate(mothers, result, F) with F = m^2(mu+ mu-) as a compiled-in
+    lambda against the menu's Mass2(1, 2) on the same chain: the events are the same code in both
+    (weights bit for bit); the functor values differ only by how m^2 is rounded (FP64: the menu's
+    separately rounded operations against nvcc's contracted ones, 1e-12; FP32_FIX: the menu's float
+    m^2 in the mother's frame against the lambda's double m^2 of the widened four-vectors, 1e-6)."""
+    n = 3000
+    d = run_mothers(mothers_program, n, precision)
+    assert d["user_w"].shape == (n,)
+    assert np.array_equal(d["user_w"], d["menu_w"])
+    tol = 1e-12 if precision == 0 else 1e-6
+    assert float(np.max(np.abs(d["user_f"] - d["menu_f"]) / np.abs(d["menu_f"]))) <= tol
+    (mm, em), (mu, eu) = d["avg_menu"], d["avg_user"]
+    assert abs(mu - mm) <= tol * abs(mm) and abs(eu - em) <= 1e-4 * em
+
+
+@pytest.mark.gpu
+def test_user_functor_with_mothers_fp32fix_within_contract(mothers_program, cuda):
+    """The FP32_FIX weights and functor values of the per-event-mother Evaluate against FP64: weights
+    within the 1e-6 relative contract of that form; m^2 of the boosted muons within 2e-6 (each
+    four-vector is within 1e-6 x the mother's gamma, about 1.14 for a J/psi from B0 -> J/psi K pi,
+    and E^2 - p^2 of the pair cancels by gamma^2)."""
+    a, b = run_mothers(mothers_program, 3000, 0), run_mothers(mothers_program, 3000, 1)
+    assert float(np.max(np.abs(b["user_w"] - a["user_w"]) / a["user_w"])) <= 1e-6
+    assert float(np.max(np.abs(b["user_f"] - a["user_f"]) / a["user_f"])) <= 2e-6
