@@ -24,8 +24,12 @@ constexpr int kAvgThreads = kTileThreads;
 __host__ __device__ constexpr bool avg_paired(int N) { return N >= 3 && N <= 5; }
 
 // Resident CTAs per SM the register allocation of the FP32_FIX tile kernels must allow (second
-// argument of __launch_bounds__; 0 leaves the choice to the compiler).
-__host__ __device__ constexpr int avg_min_ctas(int N) { return N >= 9 ? 2 : 0; }
+// argument of __launch_bounds__; 0 leaves the choice to the compiler).  AverageOn at 2^24 events,
+// ms for N = 2..10 (registers in brackets):
+//   compiler  0.181 0.276 0.376 0.496 0.790 1.329 1.653 1.951 2.335  (39..128)
+//   2 CTAs    0.179 0.282 0.411 0.524 0.825 1.378 1.647 1.952 2.278  (<= 128)
+//   3 CTAs    0.179 0.278 0.389 0.514 0.804 1.359 1.655 1.994 2.440  (<= 80)
+__host__ __device__ constexpr int avg_min_ctas(int N) { return N == 10 ? 2 : 0; }
 
 template <int N, int ENGINE>
 __global__ void __launch_bounds__(kAvgThreads)

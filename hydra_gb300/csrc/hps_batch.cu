@@ -172,8 +172,15 @@ __device__ __forceinline__ void batch_body(const BatchItemDev* __restrict__ item
     }
 }
 
+// Resident CTAs per SM the register allocation of a class kernel must allow (second argument of
+// __launch_bounds__; 0 leaves the choice to the compiler).  The N >= 7 classes held to 128
+// registers (2 CTAs per SM) took the 256-channel batch from 2.776 ms to 2.612 ms (best of the
+// autotuner's CTAs per SM each); capping from N = 8 or only N = 10 gave 2.616 and 2.635 ms, and
+// 80 registers spill 360 to 1448 bytes.
+__host__ __device__ constexpr int batch_min_ctas(int c) { return (!class_split(c) && class_n(c) >= 7) ? 2 : 0; }
+
 template <int CLS>
-__global__ void __launch_bounds__(kTileThreads)
+__global__ void __launch_bounds__(kTileThreads, batch_min_ctas(CLS))
 k_batch_f32(const BatchItemDev* __restrict__ items, BatchHeader* __restrict__ hdr, hps_stats* __restrict__ partials)
 {
     batch_body<CLS>(items, hdr, partials);

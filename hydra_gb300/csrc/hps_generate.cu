@@ -45,17 +45,17 @@ constexpr int kGenThreads = kTileThreads;
 // (the second argument of __launch_bounds__: registers are capped at 65536 / (threads x CTAs); 0
 // leaves the choice to the compiler).  Smaller CTAs wait less at the per-chunk barrier of the
 // shared random words, at the cost of (B - 1) / NT more Philox blocks per event; from N = 7 the
-// event body is long enough that 256 threads pay, and from N = 8 holding it to 80 registers (3 CTAs
-// per SM) beats the compiler's choice.  Measured at 2^24 events (ms; registers in brackets):
+// event body is long enough that 256 threads pay, and at N = 7..9 a register cap beats the
+// compiler's choice.  Measured at 2^24 events (ms; registers in brackets):
 //   N                  2      3      4      5      6      7      8      9      10
-//   128, compiler  0.172  0.289  0.399  0.514  0.813  1.522  1.874  2.460  2.944  (47..110)
-//   128, 1 CTA     0.168  0.298  0.411  0.539  0.858  1.516  1.901  2.449  2.827  (56..215)
-//   128, 6 CTAs    0.169  0.297  0.405  0.533  0.825  1.554  1.898  2.294  2.856  (<= 80)
-//   256, compiler  0.175  0.300  0.400  0.531  0.846  1.451  1.904  2.199  3.031  (47..142)
-//   256, 2 CTAs    0.176  0.323  0.500  0.566  0.924  1.557  1.973  2.307  2.516  (<= 128)
-//   256, 3 CTAs    0.176  0.327  0.440  0.562  0.851  1.470  1.788  2.096  2.649  (<= 80)
+//   128, compiler  0.169  0.287  0.396  0.506  0.794  1.438  1.770  2.223  2.838  (47..110)
+//   128, 6 CTAs    0.167  0.293  0.400  0.533  0.808  1.489  1.807  2.212  2.727  (<= 80)
+//   256, compiler  0.174  0.295  0.396  0.530  0.814  1.476  1.836  2.127  2.400  (47..110)
+//   256, 2 CTAs    0.174  0.318  0.493  0.555  0.914  1.522  1.929  2.208  2.482  (<= 128)
+//   256, 3 CTAs    0.174  0.326  0.433  0.561  0.832  1.423  1.705  2.015  2.511  (<= 80)
+//   256, 4 CTAs    0.176  0.301  0.397  0.531  0.836  1.408  1.767  2.127  2.686  (<= 64)
 __host__ __device__ constexpr int gen_threads(int N) { return N <= 6 ? 128 : kGenThreads; }
-__host__ __device__ constexpr int gen_min_ctas(int N) { return N <= 7 ? 0 : N <= 9 ? 3 : 2; }
+__host__ __device__ constexpr int gen_min_ctas(int N) { return N <= 6 || N == 10 ? 0 : N == 7 ? 4 : 3; }
 
 // Two events per thread and iteration (store_pair_f32: one word exchange for two chunks, and two
 // independent event bodies for the scheduler to interleave) pays where an event is short: at 2^24

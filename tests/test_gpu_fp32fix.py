@@ -139,3 +139,14 @@ def test_fp32fix_near_coincident_uniforms(api, torch, oracle):
     e4, ew, _, _, _ = errors(api, torch, oracle, 10, 0, 5.0, [PI] * 10, 4, first=21689202)
     print(f"\n[fp32_fix] near-coincident uniforms: four {e4:.3e}, weight {ew:.3e}")
     assert e4 <= TOL and ew <= TOL
+
+
+def test_fp32fix_weight_product_range(api, torch, oracle):
+    """From N = 7 the weight is sqrt(prod num) / prod 2a over the stages, num = (2a pd)^2, so
+    prod num spans twice the weight's range.  Event 13901751 of ten pions from M = 8 GeV (Philox
+    seed 0x3039) takes it below float's normal range (about 1e-40 after the channel's fixed
+    scaling) although its weight, 3e-8 of the maximum, is ordinary; each stage now takes an even
+    power of two out of the product.  The 128 events around it against the oracle."""
+    e4, ew, _, _, _ = errors(api, torch, oracle, 10, 0, 8.0, [PI] * 10, 128, first=13901700)
+    print(f"\n[fp32_fix] weight product range: four {e4:.3e}, weight {ew:.3e}")
+    assert e4 <= TOL and ew <= TOL
