@@ -2,7 +2,10 @@
 
 Workloads (Philox2x64-7, seed 0x3039, mother at rest), 2^26 events each:
   * ten pions: M = 5.0 GeV -> 10 x 0.13957 GeV;
-  * B0 -> J/psi K pi: M = 5.27934 GeV -> (3.0969, 0.493677, 0.13957) GeV.
+  * B0 -> J/psi K pi: M = 5.27934 GeV -> (3.0969, 0.493677, 0.13957) GeV;
+  * ten pions from the largest mother mass the batched workloads draw, sum(m) + 6 GeV: the
+    daughters with the most energy to share, where a daughter boosted forward and slowed by a
+    later stage carries the largest relative error.
 The FP64 kernels follow the reference's arithmetic operation for operation (pinned to the oracle
 at 1e-12 in test_gpu_parity.py), so they stand in for the oracle at this size, which the CPU
 oracle would need minutes for.  Events are compared in chunks of 2^22 on the GPU.
@@ -26,6 +29,7 @@ TOTAL = 1 << 26
 WORKLOADS = [
     ("ten_pions_M5", 5.0, [PI] * 10),
     ("b0_jpsi_k_pi", 5.27934, [3.0969, K, PI]),
+    ("ten_pions_sum_plus_6GeV", 10 * PI + 6.0, [PI] * 10),
 ]
 
 
