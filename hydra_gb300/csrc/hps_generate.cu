@@ -54,8 +54,10 @@ constexpr int kGenThreads = kTileThreads;
 //   256, 2 CTAs    0.174  0.318  0.493  0.555  0.914  1.522  1.929  2.208  2.482  (<= 128)
 //   256, 3 CTAs    0.174  0.326  0.433  0.561  0.832  1.423  1.705  2.015  2.511  (<= 80)
 //   256, 4 CTAs    0.176  0.301  0.397  0.531  0.836  1.408  1.767  2.127  2.686  (<= 64)
+// At N = 10 the order turns at the 2^26 events of the ten-pion workload: 10.08 ms with 2 CTAs,
+// 10.39 with 3 and 10.66 with the compiler's 110 registers, so N = 10 takes 2 CTAs.
 __host__ __device__ constexpr int gen_threads(int N) { return N <= 6 ? 128 : kGenThreads; }
-__host__ __device__ constexpr int gen_min_ctas(int N) { return N <= 6 || N == 10 ? 0 : N == 7 ? 4 : 3; }
+__host__ __device__ constexpr int gen_min_ctas(int N) { return N <= 6 ? 0 : N == 7 ? 4 : N == 10 ? 2 : 3; }
 
 // Two events per thread and iteration (store_pair_f32: one word exchange for two chunks, and two
 // independent event bodies for the scheduler to interleave) pays where an event is short: at 2^24
