@@ -215,6 +215,7 @@ def cpu_sample(seconds=3.0, n_sample=1 << 21, nthreads=0):
 
 
 REF_HARNESS = REPO / "oracle" / "_ref" / "ref_harness_omp"
+REF_HARNESS_CPP = REPO / "oracle" / "_ref" / "ref_harness_cpp"
 
 
 def host_threads():
@@ -228,10 +229,20 @@ def reference_cpu(n_sample, reps):
     (events/s of each repetition, threads), or None where the harness was not built.  The
     reference's Generate drops the weight and stores no unweight flag, so it does less per event
     than the GPU step it is compared with."""
-    if not REF_HARNESS.exists():
+    return _time_harness(REF_HARNESS, n_sample, reps, host_threads())
+
+
+def reference_cpu_single_core(n_sample=1 << 20, reps=2):
+    """The same through the reference's CPP backend (one host thread), the single-core figure of
+    the reference's CPU path; the median events/s after one warm-up, or None where not built."""
+    r = _time_harness(REF_HARNESS_CPP, n_sample, reps, 1)
+    return None if r is None else statistics.median(r[0][1:])
+
+
+def _time_harness(harness, n_sample, reps, threads):
+    if not harness.exists():
         return None
-    threads = host_threads()
-    cmd = [str(REF_HARNESS), "time", str(N_DAUGHTERS), "0", str(SEED), str(n_sample), repr(MOTHER),
+    cmd = [str(harness), "time", str(N_DAUGHTERS), "0", str(SEED), str(n_sample), repr(MOTHER),
            *map(repr, MASSES), "2", str(BW[0]), str(BW[1]), repr(BW[2]), repr(BW[3]), str(reps)]
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=900, check=True,
                        env=dict(os.environ, OMP_NUM_THREADS=str(threads)))
@@ -264,7 +275,9 @@ def run_reference(args):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded counter-based RNG)",
         "config": workload_config(n, "fp64"), "impl": "reference",
         "cpu_baseline": {"value": value, "unit": "events/s", "cores": cores, "kind": kind, "sample": sample,
-                         "port_value": port_rate, "port_sample": port_sample},
+                         "port_value": port_rate, "port_sample": port_sample,
+                         "single_core_value": reference_cpu_single_core(),
+                         "single_core_sample": "2^20 events through the reference's CPP backend, one thread"},
         "e2e": {"value": value, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -402,7 +415,9 @@ def run_gpu(args):
             cpu = {"value": statistics.median(rates[1:]), "unit": "events/s", "cores": rcores, "kind": "reference",
                    "sample": f"{1 << 22} events of the workload, Generate + AverageOn through the reference's own "
                              f"API (Hydra OMP backend), median of 3 after 1 warm-up",
-                   "port_value": rate, "port_sample": sample}
+                   "port_value": rate, "port_sample": sample,
+                   "single_core_value": reference_cpu_single_core(),
+                   "single_core_sample": "2^20 events through the reference's CPP backend, one thread"}
 
     csum = clocks.summary()
     if rank == 0:
