@@ -255,6 +255,7 @@ __device__ __forceinline__ double recomputed_weight(const double* masses, double
 struct DevFunctor {
     int kind, i, j;
     double a, b;
+    float fa, fb;     // a and b rounded to float once on the host, for the FP32_FIX functor
 };
 
 template <int N>

@@ -25,11 +25,14 @@ __host__ __device__ constexpr bool avg_paired(int N) { return N >= 3 && N <= 5; 
 
 // Resident CTAs per SM the register allocation of the FP32_FIX tile kernels must allow (second
 // argument of __launch_bounds__; 0 leaves the choice to the compiler).  AverageOn at 2^24 events,
-// ms for N = 2..10 (registers in brackets):
-//   compiler  0.181 0.276 0.376 0.496 0.790 1.329 1.653 1.951 2.335  (39..128)
-//   2 CTAs    0.179 0.282 0.411 0.524 0.825 1.378 1.647 1.952 2.278  (<= 128)
-//   3 CTAs    0.179 0.278 0.389 0.514 0.804 1.359 1.655 1.994 2.440  (<= 80)
-__host__ __device__ constexpr int avg_min_ctas(int N) { return N == 10 ? 2 : 0; }
+// ms for N = 3, 5, 9, 10 (registers in brackets):
+//   compiler  0.270 0.484 1.940 2.309  (48, 60, 128, 128)
+//   1 CTA     0.280 0.524 2.251 2.599  (72..252)
+//   2 CTAs    0.280 0.524 1.958 2.372  (<= 128)
+//   3 CTAs    0.276 0.507 1.996 2.404  (<= 80)
+// (With the functor's parameters converted to float on the device for each event, N = 10 had
+// taken 2.278 ms with 2 CTAs against 2.335 with the compiler's choice.)
+__host__ __device__ constexpr int avg_min_ctas(int) { return 0; }
 
 template <int N, int ENGINE>
 __global__ void __launch_bounds__(kAvgThreads)

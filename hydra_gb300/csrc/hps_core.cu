@@ -55,6 +55,8 @@ hps_status to_device_functor(const hps_functor* f, int n_daughters, DevFunctor* 
     out->j = f->j;
     out->a = f->a;
     out->b = f->b;
+    out->fa = static_cast<float>(f->a);
+    out->fb = static_cast<float>(f->b);
     return HPS_OK;
 }
 

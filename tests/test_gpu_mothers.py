@@ -169,3 +169,60 @@ def test_average_mothers_fp32fix(api, torch, oracle, engine):
     print(f"\n[fp32_fix AverageMothers] {engine}: rel err mean {abs(mean - rmean) / abs(rmean):.3e}")
     assert abs(mean - rmean) <= FP32_TOL * abs(rmean)
     assert abs(mean - rmean) <= 3 * sigma
+
+
+def heavy_mothers(n, seed, mass_lo, mass_hi, p_max):
+    """n mother four-vectors with masses uniform in [mass_lo, mass_hi] and momenta up to p_max in
+    random directions."""
+    rng = np.random.default_rng(seed)
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    p = d * rng.uniform(0.0, p_max, size=(n, 1))
+    m = rng.uniform(mass_lo, mass_hi, size=(n, 1))
+    return np.concatenate([np.sqrt(m * m + (p * p).sum(axis=1, keepdims=True)), p], axis=1)
+
+
+@pytest.mark.parametrize("engine", ["philox", "squares3"])
+def test_mothers_fp32fix_full_form(api, torch, oracle, engine):
+    """The N >= 7 (full float-float) form with per-event mothers: eight pions from mothers of mass
+    2.5..4 GeV (the channel's nominal 3 GeV) and momentum up to 1 GeV.  DecayMothers against the
+    oracle; EvalMothers (each event's ECM and maximum weight from its own mother, so the float-float
+    weight's fixed scalings are off by up to the mass ratio) in FP32_FIX against the FP64 form;
+    AverageMothers against the oracle.  Four-vectors within 1e-6 x the mothers' largest gamma."""
+    n = 1 << 14
+    N, M = 8, 3.0
+    m = [0.13957] * N
+    mothers = heavy_mothers(n, 23, 2.5, 4.0, 1.0)
+    eng = oracle.ENGINE_PHILOX if engine == "philox" else oracle.ENGINE_SQUARES3
+    ch = api.make_channel(m, M, 0x3039, engine)
+    och = oracle.make_channel(m, M, 0x3039, eng)
+    mo = torch.as_tensor(mothers, device="cuda")
+    gamma = float((mothers[:, 0] / np.sqrt(mothers[:, 0] ** 2 - (mothers[:, 1:] ** 2).sum(axis=1))).max())
+    # DecayMothers (the channel's ECM; boost by each mother)
+    four = torch.zeros((N, n, 4), dtype=torch.float64, device="cuda")
+    w = torch.zeros(n, dtype=torch.float64, device="cuda")
+    api.generate_mothers(ch, 0, mo, four, w, precision="fp32_fix")
+    torch.cuda.synchronize()
+    rfour, rw = oracle.generate_mothers(och, 0, mothers)
+    e4 = enorm(four.cpu().numpy(), rfour)
+    ew = float((np.abs(w.cpu().numpy() - rw) / rw).max())
+    # EvalMothers: FP32_FIX against FP64 (pinned to the reference fixtures above)
+    fn = api.functor_mass2(1, 2)
+    w32, w64 = (torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(2))
+    f32, f64 = (torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(2))
+    api.evaluate_mothers(ch, 0, mo, [fn], w32, [f32], precision="fp32_fix")
+    api.evaluate_mothers(ch, 0, mo, [fn], w64, [f64], precision="fp64")
+    torch.cuda.synchronize()
+    a, b = w32.cpu().numpy(), w64.cpu().numpy()
+    ok = b > 0
+    eew = float((np.abs(a[ok] - b[ok]) / b[ok]).max())
+    # AverageMothers
+    out = torch.zeros(3, dtype=torch.float64, device="cuda")
+    api.average_on_mothers(ch, 0, mo, api.functor_mass2(1, 2), out, precision="fp32_fix")
+    mean, m2, W = out.cpu().tolist()
+    rmean, rm2, rW = oracle.average_mothers(och, oracle.make_functor(1, 1, 2), 0, mothers)
+    print(f"\n[fp32_fix mothers N=8] {engine}: gamma {gamma:.2f}, DecayMothers four {e4:.3e} weight {ew:.3e}, "
+          f"EvalMothers weight {eew:.3e}, AverageMothers mean {abs(mean - rmean) / abs(rmean):.3e}")
+    assert e4 <= FP32_TOL * gamma and ew <= FP32_TOL
+    assert eew <= FP32_TOL
+    assert abs(mean - rmean) <= FP32_TOL * abs(rmean)
