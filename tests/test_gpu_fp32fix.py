@@ -150,3 +150,28 @@ def test_fp32fix_weight_product_range(api, torch, oracle):
     e4, ew, _, _, _ = errors(api, torch, oracle, 10, 0, 8.0, [PI] * 10, 128, first=13901700)
     print(f"\n[fp32_fix] weight product range: four {e4:.3e}, weight {ew:.3e}")
     assert e4 <= TOL and ew <= TOL
+
+
+@pytest.mark.parametrize("N,engine,M,masses", [(3, 0, 5.27934, [3.0969, K, PI]), (5, 1, 1.86484, [K, PI, PI, PI, PI]),
+                                               (8, 0, 3.0, [PI] * 8)])
+def test_fp32fix_final_boost(api, torch, oracle, N, engine, M, masses):
+    """The channel's final boost (DecayMother.h:264-269) when 0 < |beta|^2 < 1, which the C ABI
+    reaches through hps_channel.beta (the reference's own constructor makes it a no-op for a moving
+    mother, quirk Q1): beta = (0.3, -0.2, 0.5), gamma = 1.27.  Four-vectors within 1e-6 x gamma."""
+    n = 1 << 18
+    beta = (0.3, -0.2, 0.5)
+    ch = api.make_channel(masses, M, 0x3039, engine)
+    och = oracle.make_channel(masses, M, 0x3039, engine)
+    for i in range(3):
+        ch.beta[i] = beta[i]
+        och.beta[i] = beta[i]
+    four = torch.empty((N, n, 4), dtype=torch.float64, device="cuda")
+    w = torch.empty(n, dtype=torch.float64, device="cuda")
+    api.generate(ch, 0, four, w, None, precision="fp32_fix")
+    torch.cuda.synchronize()
+    rfour, rw = oracle.generate(och, 0, n)
+    gamma = 1.0 / np.sqrt(1.0 - sum(b * b for b in beta))
+    e4 = float((np.abs(four.cpu().numpy() - rfour).max(axis=2) / rfour[:, :, 0]).max())
+    ew = float((np.abs(w.cpu().numpy() - rw) / rw).max())
+    print(f"\n[fp32_fix] final boost N={N}: four {e4:.3e}, weight {ew:.3e}")
+    assert e4 <= TOL * gamma and ew <= TOL
