@@ -493,7 +493,7 @@ def precision_part(api, torch, total=1 << 26, chunk=1 << 22):
     return out
 
 
-def batch_part(api, torch, peak, n_channels=256, check_channels=32):
+def batch_part(api, torch, peak, n_channels=256, check_channels=256):
     """256 seeded channels (N uniform in 2..10, masses from the menu, events log-uniform 1e3..1e6),
     store path, one graph launch of the batched FP32_FIX kernels after the project's autotuner."""
     from hydra_gb300 import batch_bench as BB

@@ -200,3 +200,34 @@ def test_batch_single_class_empty_and_reordered(api, torch):
     plan.launch()
     assert_same_as_alone(api, torch, mix2)
     plan.close()
+
+
+def test_config4_every_event_within_contract(api, torch):
+    """The batched workload exactly as the bench runs it (256 seeded channels: N uniform in 2..10,
+    daughter masses from the menu, mother mass uniform in [1.2 sum m, sum m + 6] GeV, events
+    log-uniform 1e3..1e6, about 35 M in all): every event of the one-launch FP32_FIX batch against
+    the FP64 form of the same events, within the 1e-6 contract (four-vectors max_k |dp_k| / E,
+    weights |dw| / w)."""
+    from hydra_gb300 import batch_bench as BB
+    chans = BB.make_channels(256)
+    outs, items, hch = [], [], []
+    for N, m, M, n, seed in chans:
+        ch = api.make_channel(m, M, seed, "philox")
+        four = torch.empty((N, n, 4), dtype=torch.float64, device="cuda")
+        w = torch.empty(n, dtype=torch.float64, device="cuda")
+        outs.append((four, w))
+        hch.append(ch)
+        items.append(api.store_item(ch, 0, four, w))
+    plan = api.BatchPlan(len(items), 1)
+    plan.set_items(items)
+    plan.launch()
+    torch.cuda.synchronize()
+    e4 = ew = 0.0
+    for ch, (four, w) in zip(hch, outs):
+        f64, w64 = torch.empty_like(four), torch.empty_like(w)
+        api.generate(ch, 0, f64, w64, None, precision="fp64")
+        e4 = max(e4, float(((four - f64).abs().amax(dim=2) / f64[:, :, 0]).max()))
+        ew = max(ew, float(((w - w64).abs() / w64).max()))
+    plan.close()
+    print(f"\n[batch config 4] {sum(c[3] for c in chans)} events: four {e4:.3e}, weight {ew:.3e}")
+    assert e4 <= 1e-6 and ew <= 1e-6
