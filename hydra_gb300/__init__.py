@@ -178,7 +178,7 @@ SIGNATURES = {
     "hps_weight_flags": (_i32, [_u64, _vp, _dbl, _vp, _u64, _u64, _vp, _vp]),
     "hps_dalitz_histogram": (_i32, [_i32, _vp, _dbl, _u64, _vp, _vp, _i32, ctypes.POINTER(HpsHist2D), _vp, _vp]),
     "hps_generate_dalitz": (_i32, [ctypes.POINTER(HpsChannel), _u64, _u64, _i32, ctypes.POINTER(HpsHist2D), _vp,
-                                   _vp]),
+                                   _i32, _vp]),
     "hps_range_channel": (_i32, [ctypes.POINTER(HpsChannel), _i32, _vp, _vp, _u64]),
     "hps_generate_range": (_i32, [ctypes.POINTER(HpsChannel), _u64, _u64, _vp, _vp, _vp]),
     "hps_default_seed": (_u64, [_i32, _vp]),

@@ -310,9 +310,9 @@ def dalitz_histogram(n_daughters: int, masses: Sequence[float], max_weight: floa
 
 
 def generate_dalitz(ch: HpsChannel, first: int, n: int, hist: HpsHist2D, bins: torch.Tensor, weight_mode="phsp",
-                    stream=None) -> None:
+                    precision="fp64", stream=None) -> None:
     check(lib().hps_generate_dalitz(ctypes.byref(ch), first, n, _HIST_WEIGHTS[weight_mode], ctypes.byref(hist),
-                                    _dptr(bins), _stream_handle(stream)))
+                                    _dptr(bins), _PRECISIONS[precision], _stream_handle(stream)))
 
 
 def range_channel(masses: Sequence[float], mother: Sequence[float], seed: int) -> HpsChannel:
@@ -717,9 +717,10 @@ class PhaseSpace:
     def DalitzHistogram(self, mother, n: int, grid=(100, 100), lower=(0.0, 0.0), upper=(1.0, 1.0), pair_a=(0, 1),
                         pair_b=(1, 2), weight_mode="phsp") -> torch.Tensor:
         """Generate + Dalitz histogram fused: the events are binned where they are made and
-        never stored (FP64; weight_mode "phsp" uses the generation-time weight)."""
+        never stored (in this object's precision; weight_mode "phsp" uses the generation-time weight)."""
         bins = torch.empty(int(grid[0]) * int(grid[1]) + 2, dtype=torch.float64, device="cuda")
-        generate_dalitz(self._channel(mother), 0, n, hist2d(pair_a, pair_b, grid, lower, upper), bins, weight_mode)
+        generate_dalitz(self._channel(mother), 0, n, hist2d(pair_a, pair_b, grid, lower, upper), bins, weight_mode,
+                        self.precision)
         torch.cuda.current_stream().synchronize()
         return bins
 

@@ -7,6 +7,7 @@
 
 #include "common.h"
 #include "store.cuh"
+#include "tiles_f32.cuh"
 
 namespace hps {
 
@@ -74,6 +75,8 @@ struct DevHist {
     uint64_t g0, g1;
     double lo0, lo1, delta0, delta1;
     uint64_t nbins;          // g0 * g1 + 2
+    // the FP32_FIX form: lower edges, grid / (upper - lower) and the grid sizes as floats
+    float lo0f, lo1f, sc0f, sc1f, g0f, g1f;
 };
 
 // GetGlobalBin::operator() for two dimensions, each step in the reference's order:
@@ -120,6 +123,38 @@ __device__ __forceinline__ void dalitz_xy(const DevHist& h, const double (&p)[N]
     }
     x0 = f64::mass2(s);
     x1 = f64::mass2(t);
+}
+
+// The FP32_FIX form of both: the pair masses squared of the float four-vectors (as the FP32_FIX
+// functor forms them) and the bin from X = (x - lower) * (grid / (upper - lower)) in float, the
+// same under/overflow rules.  An event whose Dalitz variable lies within the float form's error of
+// a bin edge may fall in the neighbouring bin.
+template <int N>
+__device__ __forceinline__ void dalitz_xy_f32(const DevHist& h, const float (&p)[N][4], float& x0, float& x1)
+{
+    float s[4] = {0.0f, 0.0f, 0.0f, 0.0f}, t[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        const float ws = (k == h.a0 ? 1.0f : 0.0f) + (k == h.a1 ? 1.0f : 0.0f);
+        const float wt = (k == h.b0 ? 1.0f : 0.0f) + (k == h.b1 ? 1.0f : 0.0f);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            s[c] = fmaf(ws, p[k][c], s[c]);
+            t[c] = fmaf(wt, p[k][c], t[c]);
+        }
+    }
+    x0 = fmaf(s[0], s[0], -fmaf(s[1], s[1], fmaf(s[2], s[2], s[3] * s[3])));
+    x1 = fmaf(t[0], t[0], -fmaf(t[1], t[1], fmaf(t[2], t[2], t[3] * t[3])));
+}
+
+__device__ __forceinline__ uint64_t global_bin_f32(const DevHist& h, float x0, float x1)
+{
+    const float X0 = (x0 - h.lo0f) * h.sc0f, X1 = (x1 - h.lo1f) * h.sc1f;
+    const uint64_t nb = h.g0 * h.g1;
+    if (X0 < 0.0f && X1 < 0.0f) return nb;
+    if (X0 > h.g0f && X1 > h.g1f) return nb + 1;
+    if (!(X0 >= 0.0f && X0 < h.g0f && X1 >= 0.0f && X1 < h.g1f)) return nb + 1;
+    return static_cast<uint64_t>(X0) * h.g1 + static_cast<uint64_t>(X1);
 }
 
 // Up to kSmemBins bins each CTA keeps a private copy in shared memory and adds its non-zero
@@ -195,6 +230,32 @@ k_dalitz_generate(DevChannel ch, int mode, DevHist h, uint64_t first, uint64_t n
     hist_end(h, sink);
 }
 
+// FP32_FIX fused form: chunks of kTileThreads consecutive events with their random words shared by
+// the CTA (cta_event_words), the float event body, binned where it is made.
+template <int N, int ENGINE>
+__global__ void __launch_bounds__(kTileThreads)
+k_dalitz_generate_f32(DevChannel chd, DevChannelF ch, int mode, DevHist h, uint64_t first, uint64_t n,
+                      double* __restrict__ bins, int use_smem)
+{
+    __shared__ __align__(16) unsigned char words[WordShare<N, ENGINE, kTileThreads>::BYTES2];
+    const HistSink sink = hist_begin(h, bins, use_smem != 0);
+    const uint64_t step = (uint64_t)gridDim.x * kTileThreads;
+    int parity = 0;
+    for (uint64_t cb = (uint64_t)blockIdx.x * kTileThreads; cb < n; cb += step, parity ^= 1) {
+        uint64_t w[3 * N - 4];
+        cta_event_words<N, ENGINE, kTileThreads>(chd.key, first + cb, words, w, parity);
+        const uint64_t e = cb + threadIdx.x;
+        if (e < n) {
+            float p[N][4];
+            const f32::EventWeight ew = f32::event_from_words<N, ENGINE>(chd, ch, w, p);
+            float x0, x1;
+            dalitz_xy_f32<N>(h, p, x0, x1);
+            sink.add(global_bin_f32(h, x0, x1), mode == HPS_HIST_PHSP_WEIGHT ? ew.weight : 1.0);
+        }
+    }
+    hist_end(h, sink);
+}
+
 static hps_status hist_args(const hps_hist2d* hist, int32_t n_daughters, int32_t weight_mode, DevHist* h)
 {
     if (!hist) return set_error(HPS_ERR_BAD_ARG, "hist is NULL");
@@ -220,6 +281,12 @@ static hps_status hist_args(const hps_hist2d* hist, int32_t n_daughters, int32_t
     h->delta0 = hist->upper[0] - hist->lower[0];
     h->delta1 = hist->upper[1] - hist->lower[1];
     h->nbins = h->g0 * h->g1 + 2;
+    h->lo0f = static_cast<float>(h->lo0);
+    h->lo1f = static_cast<float>(h->lo1);
+    h->sc0f = static_cast<float>(static_cast<double>(h->g0) / h->delta0);
+    h->sc1f = static_cast<float>(static_cast<double>(h->g1) / h->delta1);
+    h->g0f = static_cast<float>(h->g0);
+    h->g1f = static_cast<float>(h->g1);
     return HPS_OK;
 }
 
@@ -315,7 +382,7 @@ hps_status hps_dalitz_histogram(int32_t n_daughters, const double* masses, doubl
 }
 
 hps_status hps_generate_dalitz(const hps_channel* channel, uint64_t first_evt, uint64_t n, int32_t weight_mode,
-                               const hps_hist2d* hist, double* bins, void* stream)
+                               const hps_hist2d* hist, double* bins, int32_t precision, void* stream)
 {
     HPS_ENTRY();
     DevChannel ch;
@@ -327,10 +394,27 @@ hps_status hps_generate_dalitz(const hps_channel* channel, uint64_t first_evt, u
     if ((st = hist_args(hist, channel->n_daughters, weight_mode, &h)) != HPS_OK) return st;
     if (!bins || !aligned(bins, 8)) return set_error(HPS_ERR_BAD_ARG, "bins NULL or misaligned");
     if (!range_ok(first_evt, n)) return set_error(HPS_ERR_BAD_ARG, "event range wraps 2^64");
+    if (precision != HPS_PREC_FP64 && precision != HPS_PREC_FP32_FIX)
+        return set_error(HPS_ERR_BAD_ARG, "unknown precision %d", precision);
     cudaStream_t s = as_stream(stream);
     if ((st = cuda_status(cudaMemsetAsync(bins, 0, h.nbins * sizeof(double), s), "cudaMemsetAsync")) != HPS_OK)
         return st;
     if (n == 0) return HPS_OK;
+    if (precision == HPS_PREC_FP32_FIX) {
+        DevChannelF chf;
+        to_device_channel_f(channel, &chf);
+#define HPS_BODY(NN, EE)                                                                                   \
+        {                                                                                                  \
+            int use_smem;                                                                                  \
+            size_t smem;                                                                                   \
+            if ((st = hist_smem_setup(k_dalitz_generate_f32<NN, EE>, h, &use_smem, &smem)) != HPS_OK) return st; \
+            k_dalitz_generate_f32<NN, EE><<<hist_grid(n, use_smem), kTileThreads, smem, s>>>(             \
+                ch, chf, weight_mode, h, first_evt, n, bins, use_smem);                                    \
+        }
+        HPS_DISPATCH_F32(channel->n_daughters, channel->engine, chf.precise, HPS_BODY)
+#undef HPS_BODY
+        return cuda_status(cudaGetLastError(), "hps_generate_dalitz launch");
+    }
 #define HPS_BODY(NN, EE)                                                                                   \
     {                                                                                                      \
         int use_smem;                                                                                      \

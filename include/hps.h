@@ -39,7 +39,7 @@ extern "C" {
 #endif
 
 #define HPS_MAX_DAUGHTERS 10
-#define HPS_ABI_VERSION 3
+#define HPS_ABI_VERSION 4
 
 typedef enum hps_status {
     HPS_OK = 0,
@@ -312,12 +312,15 @@ hps_status hps_dalitz_histogram(int32_t n_daughters, const double* masses, doubl
                                 const double* const* cols, const double* weights, int32_t weight_mode,
                                 const hps_hist2d* hist, double* bins, void* stream);
 
-/* Generate + histogram fused (FP64): the events of hps_generate(channel, first_evt, n) binned as
- * hps_dalitz_histogram bins them, never stored.  weight_mode HPS_HIST_UNIT or
+/* Generate + histogram fused: the events of hps_generate(channel, first_evt, n, ..., precision)
+ * binned as hps_dalitz_histogram bins them, never stored.  weight_mode HPS_HIST_UNIT or
  * HPS_HIST_PHSP_WEIGHT (the generation-time weight, which differs from the recomputed
- * PhaseSpaceWeight by rounding only). */
+ * PhaseSpaceWeight by rounding only).  HPS_PREC_FP64: the reference's arithmetic throughout.
+ * HPS_PREC_FP32_FIX: the FP32_FIX events, their pair masses squared and bins formed in float
+ * (X = (x - lower) * (grid / (upper - lower))); every event is counted, and one whose Dalitz
+ * variable lies within the float form's error of a bin edge may land in the neighbouring bin. */
 hps_status hps_generate_dalitz(const hps_channel* channel, uint64_t first_evt, uint64_t n, int32_t weight_mode,
-                               const hps_hist2d* hist, double* bins, void* stream);
+                               const hps_hist2d* hist, double* bins, int32_t precision, void* stream);
 
 /* phase_space_range (hydra/detail/PhaseSpaceRange.inl:46-73): the lazy range of GenerateDecay
  * (functors/GenerateDecay.h:222-334) with thrust's minstd_rand.  hps_range_channel sets up the

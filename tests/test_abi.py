@@ -36,7 +36,7 @@ def test_library_exports_every_declared_symbol(hps):
 
 
 def test_abi_version(hps):
-    assert hps.lib().hps_abi_version() == 3
+    assert hps.lib().hps_abi_version() == 4
 
 
 @pytest.mark.parametrize("name", GEN_GOLDEN)
@@ -157,8 +157,10 @@ def test_consumer_arguments_rejected_before_launch(hps):
     ch = api.make_channel([0.1, 0.2, 0.3], 1.0, 1)
     st = lib.hps_generate_range(ctypes.byref(ch), 0, 10, ctypes.cast(cols, ctypes.c_void_p), None, None)
     assert st == hps.ERR_BAD_ARG and b"hps_range_channel" in lib.hps_last_error()
-    st = lib.hps_generate_dalitz(ctypes.byref(ch), 0, 10, hps.HIST_COLUMN, ctypes.byref(h), bins, None)
+    st = lib.hps_generate_dalitz(ctypes.byref(ch), 0, 10, hps.HIST_COLUMN, ctypes.byref(h), bins, 0, None)
     assert st == hps.ERR_BAD_ARG
+    st = lib.hps_generate_dalitz(ctypes.byref(ch), 0, 10, hps.HIST_UNIT, ctypes.byref(h), bins, 7, None)
+    assert st == hps.ERR_BAD_ARG and b"precision" in lib.hps_last_error()
     # GenerateDecay has no checks; the range set-up reports what would otherwise be NaNs
     with pytest.raises(hps.HpsError):
         api.range_channel([0.1, 0.2, 0.3], [0.5, 0.0, 0.0, 0.0], 5)

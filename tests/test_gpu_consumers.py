@@ -99,6 +99,38 @@ def test_dalitz_fused_matches_stored(api, torch, oracle, engine):
 
 
 @pytest.mark.parametrize("name", EXTRA_GOLDEN)
+@pytest.mark.parametrize("N,engine,M,masses", [(3, "philox", 1.86484, [0.493677, 0.13957, 0.13957]),
+                                               (3, "squares3", 5.27934, [3.0969, 0.493677, 0.13957]),
+                                               (5, "philox", 1.86484, [0.493677] + [0.13957] * 4),
+                                               (8, "philox", 3.0, [0.13957] * 8)])
+def test_dalitz_fused_fp32fix(api, torch, N, engine, M, masses):
+    """The FP32_FIX fused histogram against the FP64 one of the same events (which the test above
+    pins to the oracle): every event counted; the only differences are events near a bin edge
+    moving to the neighbouring bin.  A pair mass squared carries about 1e-7 of the pair's energy
+    squared as float rounding, so about that fraction of a bin width around each of the 64 + 48
+    edges is in doubt: |dcount| summed over the bins stays below 1e-3 of n.  The weighted totals
+    agree within 1e-6."""
+    n = 1 << 21
+    ch = api.make_channel(masses, M, 0x3039, engine)
+    lo = ((masses[0] + masses[1]) ** 2, (masses[1] + masses[2]) ** 2)
+    hi = ((M - sum(masses[2:])) ** 2, (M - masses[0] - sum(masses[3:])) ** 2)
+    h = api.hist2d((0, 1), (1, 2), (64, 48), lo, hi)
+    out = {}
+    for prec in ("fp64", "fp32_fix"):
+        for mode in ("unit", "phsp"):
+            bins = torch.empty(64 * 48 + 2, dtype=torch.float64, device="cuda")
+            api.generate_dalitz(ch, 0, n, h, bins, mode, prec)
+            out[prec, mode] = bins.cpu().numpy()
+    c64, c32 = out["fp64", "unit"], out["fp32_fix", "unit"]
+    assert c32.sum() == n and c64.sum() == n
+    moved = float(np.abs(c32 - c64).sum())
+    w64, w32 = out["fp64", "phsp"], out["fp32_fix", "phsp"]
+    print(f"\n[fp32_fix dalitz] N={N} {engine}: {moved:.0f} of {n} counts moved, weighted total "
+          f"{abs(w32.sum() - w64.sum()) / w64.sum():.2e}")
+    assert moved <= 1e-3 * n
+    assert abs(w32.sum() - w64.sum()) <= 1e-6 * w64.sum()
+
+
 def test_phase_space_range(api, torch, name):
     g = load_golden(name)
     w, four = api.phase_space_range(list(g["range_mother"]), list(g["masses"]), int(g["rseed"]), int(g["n"]))
