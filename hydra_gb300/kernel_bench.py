@@ -9,7 +9,8 @@ Channels (Philox, seed 0x3039, mother at rest):
   10   ten pions             M = 5.0,     m = 0.13957 x 10
 The functor of AverageOn and Evaluate is |BW(m_01)|^2 (m0 = 0.8955, G0 = 0.0473); Evaluate
 stores the generation-time weight and the functor value (16 bytes per event), Generate the
-Decays columns, the weight and the unweight flag (32N + 9 bytes per event).
+Decays columns, the weight and the unweight flag (32N + 9 bytes per event); dalitz bins
+m^2(d0 d1) against m^2(d1 d2) on a 64 x 48 grid as the events are made (N >= 3).
 
 Prints one JSON line: ms per call (CUDA events, mean of --steps calls after --warmup), events/s
 and, for the storing forms, the GB/s of algorithmic bytes written.
@@ -36,7 +37,7 @@ CHANNELS = {
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--op", choices=["generate", "average", "evaluate"], default="evaluate")
+    ap.add_argument("--op", choices=["generate", "average", "evaluate", "dalitz"], default="evaluate")
     ap.add_argument("--n-daughters", default="5", help="N, or a comma-separated list of N (one line each)")
     ap.add_argument("--events", type=int, default=1 << 24)
     ap.add_argument("--precision", choices=["fp64", "fp32_fix"], default="fp32_fix")
@@ -81,6 +82,16 @@ def run(ap, args, N):
                 api.generate(ch, 0, four, None, None, precision=args.precision)
             else:
                 api.generate(ch, 0, four, w, fl, precision=args.precision)
+    elif args.op == "dalitz":
+        # Generate + Dalitz histogram fused: m^2(d0 d1) against m^2(d1 d2) on a 64 x 48 grid over
+        # their kinematic ranges, weighted by the generation-time weight; nothing stored
+        lo = ((masses[0] + masses[1]) ** 2, (masses[1] + masses[2]) ** 2)
+        hi = ((M - sum(masses[2:])) ** 2, (M - masses[0] - sum(masses[3:])) ** 2)
+        hist = api.hist2d((0, 1), (1, 2), (64, 48), lo, hi)
+        bins = torch.empty(64 * 48 + 2, dtype=torch.float64, device=dev)
+
+        def step():
+            api.generate_dalitz(ch, 0, n, hist, bins, "phsp", args.precision)
     elif args.op == "average":
         out = torch.empty(3, dtype=torch.float64, device=dev)
         ws = torch.empty(api.average_on_workspace_size(n), dtype=torch.uint8, device=dev)
