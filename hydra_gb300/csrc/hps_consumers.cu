@@ -231,9 +231,10 @@ k_dalitz_generate(DevChannel ch, int mode, DevHist h, uint64_t first, uint64_t n
 }
 
 // FP32_FIX fused form: chunks of kTileThreads consecutive events with their random words shared by
-// the CTA (cta_event_words), the float event body, binned where it is made.
+// the CTA (cta_event_words), the float event body, binned where it is made.  From N = 9 the body
+// is held to 128 registers (two CTAs per SM; the compiler's choice, 136, leaves one).
 template <int N, int ENGINE>
-__global__ void __launch_bounds__(kTileThreads)
+__global__ void __launch_bounds__(kTileThreads, N >= 9 ? 2 : 0)
 k_dalitz_generate_f32(DevChannel chd, DevChannelF ch, int mode, DevHist h, uint64_t first, uint64_t n,
                       double* __restrict__ bins, int use_smem)
 {
