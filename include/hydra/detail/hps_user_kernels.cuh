@@ -33,6 +33,7 @@
 #include "../../../hydra_gb300/csrc/genbod.cuh"
 #include "../../../hydra_gb300/csrc/genbod_f32.cuh"
 #include "../../../hydra_gb300/csrc/store.cuh"
+#include "../../../hydra_gb300/csrc/tiles_f32.cuh"
 
 namespace hydra {
 namespace detail {
@@ -146,6 +147,106 @@ __device__ __forceinline__ double event_mother(const hps::DevChannel& ch, const 
         }
         return ew.weight;
     }
+}
+
+// AverageOn in the FP32_FIX form: the tile fold of hps_average_on's FP32_FIX kernels
+// (tiles_f32.cuh average_tile_f32) with the user's functor.  The CTA shares the random words of
+// each chunk of kThreads events (about one Philox block per event instead of ceil((3N-4)/2)); each
+// thread keeps float-float sums of P, P d and P d^2, P = prod(pdk) of the event and d = f - K0, K0
+// the functor's value at the call's first event (k_user_shift_f32, read from *k0); the tile's sums,
+// scaled by the maximum weight, go to partials as hps_sums, and k_average_final_sums forms
+// (K0 + S1/W, S2 - S1^2/W, W).  The functor sees the widened four-vectors, as in k_average_tiles.
+template <int N, int ENGINE, typename V, typename F>
+__device__ __forceinline__ float user_value_f32(const hps::DevChannel& ch, const hps::DevChannelF& chf, const F& f,
+                                                const float (&q)[N][4])
+{
+    double p[N][4];
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        p[k][0] = hps::f32::widen_pos(q[k][0]);
+#pragma unroll
+        for (int c = 1; c < 4; ++c) p[k][c] = hps::f32::widen(q[k][c]);
+    }
+    return static_cast<float>(static_cast<double>(f(event_tuple<V>(p))));
+}
+
+template <int N, int ENGINE, typename V, typename F>
+__global__ void __launch_bounds__(kThreads)
+k_average_tiles_f32(hps::DevChannel ch, hps::DevChannelF chf, F f, uint64_t first, uint64_t n, uint64_t ntiles,
+                    const float* __restrict__ k0, hps_stats* __restrict__ partials)
+{
+    static_assert(kThreads == hps::kTileThreads, "the word exchange is sized for the tile's CTA");
+    __shared__ __align__(16) unsigned char smem[hps::WordShare<N, ENGINE, kThreads>::BYTES2];
+    const float K0 = *k0;
+    for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        float swh = 0.0f, swl = 0.0f, s1h = 0.0f, s1l = 0.0f, s2h = 0.0f, s2l = 0.0f;
+        const uint64_t base = t * HPS_AVG_TILE;
+        for (int k = 0; k < kPerThread; ++k) {
+            const uint64_t cb = base + (uint64_t)k * kThreads;
+            if (cb >= n) break;                                          // CTA-uniform
+            uint64_t w[3 * N - 4];
+            hps::cta_event_words<N, ENGINE, kThreads>(ch.key, first + cb, smem, w, k);
+            const uint64_t e = cb + threadIdx.x;
+            if (e < n) {
+                float q[N][4];
+                const hps::f32::EventWeight ew = hps::f32::event_from_words<N, ENGINE>(ch, chf, w, q);
+                const float d = user_value_f32<N, ENGINE, V>(ch, chf, f, q) - K0;
+                const float h1 = ew.prod_hi * d;
+                const float l1 = fmaf(ew.prod_lo, d, fmaf(ew.prod_hi, d, -h1));
+                const float h2 = h1 * d;
+                const float l2 = fmaf(l1, d, fmaf(h1, d, -h2));
+                hps::ff_add(swh, swl, ew.prod_hi, ew.prod_lo);
+                hps::ff_add(s1h, s1l, h1, l1);
+                hps::ff_add(s2h, s2l, h2, l2);
+            }
+        }
+        hps::hps_sums acc;
+        acc.w = ch.max_weight * (hps::f32::widen(swh) + hps::f32::widen(swl));
+        acc.s1 = ch.max_weight * (hps::f32::widen(s1h) + hps::f32::widen(s1l));
+        acc.s2 = ch.max_weight * (hps::f32::widen(s2h) + hps::f32::widen(s2l));
+        const hps::hps_sums r = hps::block_reduce_sums<kThreads>(acc);
+        if (threadIdx.x == 0) reinterpret_cast<hps::hps_sums*>(partials)[t] = r;
+        __syncthreads();          // the next tile's word exchange reuses the buffers
+    }
+}
+
+// The FP32_FIX tiles' sums in a fixed order (thread j adds tiles j, j + kFinal, ...; the fixed CTA
+// tree adds the threads' sums) and the call's StatsPHSP from them.
+template <int = 0>
+__global__ void __launch_bounds__(kFinal)
+k_average_final_sums(const hps_stats* __restrict__ partials, uint64_t ntiles, const float* __restrict__ k0,
+                     hps_stats* __restrict__ out)
+{
+    const float K0 = *k0;
+    const hps::hps_sums* tiles = reinterpret_cast<const hps::hps_sums*>(partials);
+    hps::hps_sums acc{0.0, 0.0, 0.0};
+    for (uint64_t t = threadIdx.x; t < ntiles; t += kFinal) {
+        const hps::hps_sums v = tiles[t];
+        acc.s1 += v.s1; acc.s2 += v.s2; acc.w += v.w;
+    }
+    const hps::hps_sums tot = hps::block_reduce_sums<kFinal>(acc);
+    if (threadIdx.x == 0) {
+        hps_stats r{0.0, 0.0, 0.0};
+        if (tot.w != 0.0) {
+            const double q = tot.s1 / tot.w;
+            r.w = tot.w;
+            r.mean = hps::f32::widen(K0) + q;
+            r.m2 = fma(-tot.s1, q, tot.s2);
+        }
+        *out = r;
+    }
+}
+
+// The functor's value at one event in the FP32_FIX form (the shift K0 of the call's first event).
+template <int N, int ENGINE, typename V, typename F>
+__global__ void k_user_shift_f32(hps::DevChannel ch, hps::DevChannelF chf, F f, uint64_t first, float* __restrict__ k0)
+{
+    if (threadIdx.x != 0) return;
+    uint64_t w[3 * N - 4];
+    hps::event_words<N, hps::engine_of(ENGINE)>(ch.key, first, w);
+    float q[N][4];
+    hps::f32::event_from_words<N, ENGINE>(ch, chf, w, q);
+    *k0 = user_value_f32<N, ENGINE, V>(ch, chf, f, q);
 }
 
 // AverageOn(mothers, functor) (AverageMothers): event e boosted by mothers[e]; the functor sees
