@@ -156,10 +156,17 @@ __device__ __forceinline__ double event_mother(const hps::DevChannel& ch, const 
 // the functor's value at the call's first event (k_user_shift_f32, read from *k0); the tile's sums,
 // scaled by the maximum weight, go to partials as hps_sums, and k_average_final_sums forms
 // (K0 + S1/W, S2 - S1^2/W, W).  The functor sees the widened four-vectors, as in k_average_tiles.
-template <int N, int ENGINE, typename V, typename F>
-__device__ __forceinline__ float user_value_f32(const hps::DevChannel& ch, const hps::DevChannelF& chf, const F& f,
-                                                const float (&q)[N][4])
+// The functor's value at one FP32_FIX event, rounded to float.  With MOTHERS the event is first
+// boosted into the frame of its mother mo and the functor sees (mother, daughters...).
+template <int N, int ENGINE, bool MOTHERS, typename V, typename F>
+__device__ __forceinline__ float user_value_f32(const hps::DevChannelF& chf, const F& f, float (&q)[N][4],
+                                                const double* __restrict__ mothers, uint64_t e)
 {
+    double mo[4] = {0.0, 0.0, 0.0, 0.0};
+    if constexpr (MOTHERS) {
+        for (int c = 0; c < 4; ++c) mo[c] = mothers[4 * e + c];
+        hps::f32::boost_to_mother<N>(q, chf.m2, hps::f32::mother_frame(mo));
+    }
     double p[N][4];
 #pragma unroll
     for (int k = 0; k < N; ++k) {
@@ -167,13 +174,17 @@ __device__ __forceinline__ float user_value_f32(const hps::DevChannel& ch, const
 #pragma unroll
         for (int c = 1; c < 4; ++c) p[k][c] = hps::f32::widen(q[k][c]);
     }
-    return static_cast<float>(static_cast<double>(f(event_tuple<V>(p))));
+    if constexpr (MOTHERS)
+        return static_cast<float>(static_cast<double>(f(as_tuple_m<V>(mo, p, std::make_index_sequence<N>{}))));
+    else
+        return static_cast<float>(static_cast<double>(f(event_tuple<V>(p))));
 }
 
-template <int N, int ENGINE, typename V, typename F>
+template <int N, int ENGINE, bool MOTHERS, typename V, typename F>
 __global__ void __launch_bounds__(kThreads)
 k_average_tiles_f32(hps::DevChannel ch, hps::DevChannelF chf, F f, uint64_t first, uint64_t n, uint64_t ntiles,
-                    const float* __restrict__ k0, hps_stats* __restrict__ partials)
+                    const float* __restrict__ k0, hps_stats* __restrict__ partials,
+                    const double* __restrict__ mothers = nullptr)
 {
     static_assert(kThreads == hps::kTileThreads, "the word exchange is sized for the tile's CTA");
     __shared__ __align__(16) unsigned char smem[hps::WordShare<N, ENGINE, kThreads>::BYTES2];
@@ -190,7 +201,7 @@ k_average_tiles_f32(hps::DevChannel ch, hps::DevChannelF chf, F f, uint64_t firs
             if (e < n) {
                 float q[N][4];
                 const hps::f32::EventWeight ew = hps::f32::event_from_words<N, ENGINE>(ch, chf, w, q);
-                const float d = user_value_f32<N, ENGINE, V>(ch, chf, f, q) - K0;
+                const float d = user_value_f32<N, ENGINE, MOTHERS, V>(chf, f, q, mothers, e) - K0;
                 const float h1 = ew.prod_hi * d;
                 const float l1 = fmaf(ew.prod_lo, d, fmaf(ew.prod_hi, d, -h1));
                 const float h2 = h1 * d;
@@ -237,16 +248,18 @@ k_average_final_sums(const hps_stats* __restrict__ partials, uint64_t ntiles, co
     }
 }
 
-// The functor's value at one event in the FP32_FIX form (the shift K0 of the call's first event).
-template <int N, int ENGINE, typename V, typename F>
-__global__ void k_user_shift_f32(hps::DevChannel ch, hps::DevChannelF chf, F f, uint64_t first, float* __restrict__ k0)
+// The functor's value at one event in the FP32_FIX form (the shift K0 of the call's first event,
+// with its mother mothers[0] in the per-event-mother form).
+template <int N, int ENGINE, bool MOTHERS, typename V, typename F>
+__global__ void k_user_shift_f32(hps::DevChannel ch, hps::DevChannelF chf, F f, uint64_t first, float* __restrict__ k0,
+                                 const double* __restrict__ mothers = nullptr)
 {
     if (threadIdx.x != 0) return;
     uint64_t w[3 * N - 4];
     hps::event_words<N, hps::engine_of(ENGINE)>(ch.key, first, w);
     float q[N][4];
     hps::f32::event_from_words<N, ENGINE>(ch, chf, w, q);
-    *k0 = user_value_f32<N, ENGINE, V>(ch, chf, f, q);
+    *k0 = user_value_f32<N, ENGINE, MOTHERS, V>(chf, f, q, mothers, 0);
 }
 
 // AverageOn(mothers, functor) (AverageMothers): event e boosted by mothers[e]; the functor sees
@@ -304,11 +317,39 @@ template <int N, int ENGINE, int PREC, typename V, typename Fs, int K>
 __global__ void __launch_bounds__(kThreads)
 k_evaluate(hps::DevChannel ch, hps::DevChannelF chf, Fs fs, OutColumns<K> out, uint64_t first, uint64_t n)
 {
-    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < n; e += (uint64_t)gridDim.x * blockDim.x) {
-        double p[N][4];
-        const double w = event<N, ENGINE, PREC>(ch, chf, first + e, p);
-        out.p[0][e] = w;
-        eval_each<0, V>(fs, p, out.p, e);
+    if constexpr (PREC == HPS_PREC_FP64) {
+        for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < n;
+             e += (uint64_t)gridDim.x * blockDim.x) {
+            double p[N][4];
+            const double w = event<N, ENGINE, PREC>(ch, chf, first + e, p);
+            out.p[0][e] = w;
+            eval_each<0, V>(fs, p, out.p, e);
+        }
+    } else {
+        // chunks of kThreads consecutive events whose random words the CTA shares (about one Philox
+        // block per event instead of ceil((3N - 4) / 2))
+        static_assert(kThreads == hps::kTileThreads, "the word exchange is sized for the tile's CTA");
+        __shared__ __align__(16) unsigned char smem[hps::WordShare<N, ENGINE, kThreads>::BYTES2];
+        const uint64_t step = (uint64_t)gridDim.x * kThreads;
+        int parity = 0;
+        for (uint64_t cb = (uint64_t)blockIdx.x * kThreads; cb < n; cb += step, parity ^= 1) {
+            uint64_t w[3 * N - 4];
+            hps::cta_event_words<N, ENGINE, kThreads>(ch.key, first + cb, smem, w, parity);
+            const uint64_t e = cb + threadIdx.x;
+            if (e < n) {
+                float q[N][4];
+                const hps::f32::EventWeight ew = hps::f32::event_from_words<N, ENGINE>(ch, chf, w, q);
+                double p[N][4];
+#pragma unroll
+                for (int k = 0; k < N; ++k) {
+                    p[k][0] = hps::f32::widen_pos(q[k][0]);
+#pragma unroll
+                    for (int c = 1; c < 4; ++c) p[k][c] = hps::f32::widen(q[k][c]);
+                }
+                out.p[0][e] = ew.weight;
+                eval_each<0, V>(fs, p, out.p, e);
+            }
+        }
     }
 }
 

@@ -762,8 +762,8 @@ public:
             if (ntiles) {
                 detail::user::with_engine<N>(lc, prec, [&](auto E) {
                     constexpr int EE = decltype(E)::value;
-                    detail::user::k_user_shift_f32<N, EE, Vector4R><<<1, 32>>>(lc.ch, lc.chf, functor, 0, k0.p);
-                    detail::user::k_average_tiles_f32<N, EE, Vector4R>
+                    detail::user::k_user_shift_f32<N, EE, false, Vector4R><<<1, 32>>>(lc.ch, lc.chf, functor, 0, k0.p);
+                    detail::user::k_average_tiles_f32<N, EE, false, Vector4R>
                         <<<grid, detail::user::kThreads>>>(lc.ch, lc.chf, functor, 0, n, ntiles, k0.p, part.p);
                 });
             } else {
@@ -938,18 +938,31 @@ public:
         detail::DeviceBuffer<hps_stats> part(ntiles ? ntiles : 1), out(1);
         const unsigned grid = static_cast<unsigned>(ntiles < 152u * 16u ? (ntiles ? ntiles : 1) : 152u * 16u);
         const int32_t prec = fPrecision;
-        if (ntiles) {
-            detail::user::with_engine<N>(lc, prec, [&](auto E) {
-                constexpr int EE = decltype(E)::value;
-                if (prec == HPS_PREC_FP32_FIX)
-                    detail::user::k_average_mothers_tiles<N, EE, HPS_PREC_FP32_FIX, Vector4R>
-                        <<<grid, detail::user::kThreads>>>(lc.ch, lc.chf, functor, mo, 0, n, ntiles, part.p);
-                else
+        if (prec == HPS_PREC_FP32_FIX) {
+            // the shifted float-float tile sums of the library's FP32_FIX AverageMothers
+            detail::DeviceBuffer<float> k0(1);
+            if (ntiles) {
+                detail::user::with_engine<N>(lc, prec, [&](auto E) {
+                    constexpr int EE = decltype(E)::value;
+                    detail::user::k_user_shift_f32<N, EE, true, Vector4R>
+                        <<<1, 32>>>(lc.ch, lc.chf, functor, 0, k0.p, mo);
+                    detail::user::k_average_tiles_f32<N, EE, true, Vector4R>
+                        <<<grid, detail::user::kThreads>>>(lc.ch, lc.chf, functor, 0, n, ntiles, k0.p, part.p, mo);
+                });
+            } else {
+                detail::throw_cuda(cudaMemset(k0.p, 0, sizeof(float)), "cudaMemset");
+            }
+            detail::user::k_average_final_sums<><<<1, detail::user::kFinal>>>(part.p, ntiles, k0.p, out.p);
+        } else {
+            if (ntiles) {
+                detail::user::with_engine<N>(lc, prec, [&](auto E) {
+                    constexpr int EE = decltype(E)::value;
                     detail::user::k_average_mothers_tiles<N, EE, HPS_PREC_FP64, Vector4R>
                         <<<grid, detail::user::kThreads>>>(lc.ch, lc.chf, functor, mo, 0, n, ntiles, part.p);
-            });
+                });
+            }
+            detail::user::k_average_final<><<<1, detail::user::kFinal>>>(part.p, ntiles, out.p);
         }
-        detail::user::k_average_final<><<<1, detail::user::kFinal>>>(part.p, ntiles, out.p);
         detail::throw_cuda(cudaGetLastError(), "AverageOn launch");
         hps_stats st;
         detail::throw_cuda(cudaMemcpy(&st, out.p, sizeof(st), cudaMemcpyDeviceToHost), "cudaMemcpy");
