@@ -41,13 +41,13 @@ __device__ __forceinline__ void store_event_f32(const float (&p)[N][4], const f3
     if (vec32) {
 #pragma unroll
         for (int k = 0; k < N; ++k)
-            st_v4_f64(cols.p[k] + 4 * e, f32::widen_pos(p[k][0]), f32::widen(p[k][1]), f32::widen(p[k][2]),
-                      f32::widen(p[k][3]));
+            st_v4_f64(cols.p[k] + 4 * e, f32::widen_pos(p[k][0]), f32::widen_nz(p[k][1]), f32::widen_nz(p[k][2]),
+                      f32::widen_nz(p[k][3]));
     } else {
 #pragma unroll
         for (int k = 0; k < N; ++k) {
-            st_v2_f64(cols.p[k] + 4 * e, f32::widen_pos(p[k][0]), f32::widen(p[k][1]));
-            st_v2_f64(cols.p[k] + 4 * e + 2, f32::widen(p[k][2]), f32::widen(p[k][3]));
+            st_v2_f64(cols.p[k] + 4 * e, f32::widen_pos(p[k][0]), f32::widen_nz(p[k][1]));
+            st_v2_f64(cols.p[k] + 4 * e + 2, f32::widen_nz(p[k][2]), f32::widen_nz(p[k][3]));
         }
     }
     if (weights) weights[e] = ew.weight;
@@ -131,7 +131,8 @@ __device__ __forceinline__ void store_half_f32(const DevChannel& chd, const DevC
 #pragma unroll
     for (int k = 0; k < N; ++k) {
         if (!f32::owns_pair<HALF>(k >> 1)) continue;
-        const double v[4] = {f32::widen_pos(p[k][0]), f32::widen(p[k][1]), f32::widen(p[k][2]), f32::widen(p[k][3])};
+        const double v[4] = {f32::widen_pos(p[k][0]), f32::widen_nz(p[k][1]), f32::widen_nz(p[k][2]),
+                             f32::widen_nz(p[k][3])};
         store_vec4(cols.p[k], e, v, vec32);
     }
     if constexpr (HALF == 0) {
