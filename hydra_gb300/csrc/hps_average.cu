@@ -32,6 +32,9 @@ __host__ __device__ constexpr bool avg_paired(int N) { return N >= 3 && N <= 5; 
 //   3 CTAs    0.276 0.507 1.996 2.404  (<= 80)
 // (With the functor's parameters converted to float on the device for each event, N = 10 had
 // taken 2.278 ms with 2 CTAs against 2.335 with the compiler's choice.)
+// With the current body, N = 2..6 (ms): compiler 0.180 0.271 0.368 0.488 0.788; 5 CTAs (48
+// registers) 0.186 0.288 0.379 0.492 0.822; 6 CTAs (40 registers, spilling at N = 5, 6) 0.191 0.286
+// 0.382 0.514 0.843.
 __host__ __device__ constexpr int avg_min_ctas(int) { return 0; }
 
 template <int N, int ENGINE>

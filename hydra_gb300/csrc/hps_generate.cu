@@ -56,6 +56,10 @@ constexpr int kGenThreads = kTileThreads;
 //   256, 4 CTAs    0.176  0.301  0.397  0.531  0.836  1.408  1.767  2.127  2.686  (<= 64)
 // At N = 10 the order turns at the 2^26 events of the ten-pion workload: 10.08 ms with 2 CTAs,
 // 10.39 with 3 and 10.66 with the compiler's 110 registers, so N = 10 takes 2 CTAs.
+// With the current event body, N = 2..6 at 2^24 events (ms): the compiler's 44..64 registers
+// 0.165 0.276 0.382 0.487 0.773; 10 CTAs (48 registers) 0.165 0.277 0.385 0.496 0.782; 12 CTAs
+// (40 registers, spilling at N = 3, 4, 6) 0.166 0.277 0.399 0.499 0.827.  More resident warps do
+// not pay for the tighter schedule, so N <= 6 keeps the compiler's choice.
 __host__ __device__ constexpr int gen_threads(int N) { return N <= 6 ? 128 : kGenThreads; }
 __host__ __device__ constexpr int gen_min_ctas(int N) { return N <= 6 ? 0 : N == 7 ? 4 : N == 10 ? 2 : 3; }
 
