@@ -1,17 +1,19 @@
-// hps_batch.cu -- many channels of different N in one persistent, graph-captured launch.
+// hps_batch.cu -- many channels of different N in one CUDA-graph launch of persistent kernels.
 //
 // The items of a plan are cut into work units: a store item into units of store_tile events,
-// an AverageOn item into tiles of HPS_AVG_TILE events.  Items are grouped by register class of N
-// (2-5, 6-7, 8-9, 10): one persistent kernel per class, so a class runs at the occupancy its own
-// register count allows (one kernel over every N would hold every channel to the registers of
-// N = 10).  The class kernels run as parallel branches of the graph, so the SMs one class frees
-// at its end take CTAs of the others.  A class kernel's 256-thread CTAs take units from the
-// class's device counter; each unit dispatches on (N, engine, mode) to the same work-unit
-// functions the single-channel FP32_FIX kernels use (tiles_f32.cuh), so an item's outputs do not
-// depend on what else is in the batch.  A last kernel merges each AverageOn item's tile partials
-// with the fixed tree of hps_average_on.  Counter reset, class kernels and merge are captured
-// once into a CUDA graph; the item table and its header live in device memory, so new items need
-// no re-capture.
+// an AverageOn item into tiles of HPS_AVG_TILE events.  Items are grouped by register class: one
+// persistent kernel per (N, form, mode), so a class runs at the occupancy its own register count
+// allows (one kernel over every N would hold every channel to the registers of N = 10, and one
+// kernel for both modes would hold the store path to the registers of the AverageOn tile).  The
+// class kernels run as parallel branches of the graph, so the SMs one class frees at its end take
+// CTAs of the others.  A class kernel's 256-thread CTAs take units from the class's device
+// counter; each unit dispatches on (N, engine) to the same work-unit functions the single-channel
+// FP32_FIX kernels use (tiles_f32.cuh), so an item's outputs do not depend on what else is in the
+// batch.  A last kernel merges each AverageOn item's tile partials with the fixed tree of
+// hps_average_on.  Counter reset, class kernels and merge are built once into a CUDA graph; the
+// item table and its header live in device memory, so new items need no new graph, and each
+// class kernel's grid is set from its unit count when the items change (a class with no units
+// launches one CTA).
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -41,31 +43,30 @@ struct BatchItemDev {
     int32_t mode, N, engine, vec32;
 };
 
-// (N = 7 and 8 were once capped at 80 registers for 3 CTAs per SM; with the float-float weight and
-// boosts that cap spills 184 and 356 bytes per thread, so every class runs uncapped.)
-// Register classes: one per N (class c < 9 holds N = c + 2), and for N = 4..6 one more each for
-// the channels that take the float-float boosts (classes 9..11: N = c - 5), which need more
-// registers than the plain form of the same N.  Each class kernel carries both engines and both
-// modes of its N; ptxas gives them 60 (N = 2) to 128 (N = 9, 10) registers, against 128 for a
-// kernel over every N.
-// With threads_per_event = 2, the store items of N = 7..10 go to classes 12..15 (N = c - 5),
-// whose kernels run two threads per event (store_chunk_split_f32).  Half of the daughters per
-// thread does not lower the register count much: the event's random words (3N - 4 64-bit values),
-// the stage momenta and the float-float weight are held by both threads; ptxas gives the split
-// classes 128 registers like the one-thread classes of N = 7..10, and a 3-CTA bound (80
-// registers) spills 72 to 296 bytes per thread.
-constexpr int kBatchClasses = 16;
-__host__ __device__ constexpr int class_n(int c) { return c < 9 ? c + 2 : c - 5; }
-__host__ __device__ constexpr bool class_ff(int c) { return c >= 9 && c < 12; }
-__host__ __device__ constexpr bool class_split(int c) { return c >= 12; }
+// Register classes of the store items: one per N (class c < 9 holds N = c + 2), and for N = 4..6
+// one more each for the channels that take the float-float boosts (classes 9..11: N = c - 5),
+// which need more registers than the plain form of the same N.  With threads_per_event = 2, the
+// store items of N = 7..10 go to classes 12..15 (N = c - 5), whose kernels run two threads per
+// event (store_chunk_split_f32).  Half of the daughters per thread does not lower the register
+// count much: the event's random words (3N - 4 64-bit values), the stage momenta and the
+// float-float weight are held by both threads; ptxas gives the split classes 128 registers, and a
+// 3-CTA bound (80 registers) spills 72 to 296 bytes per thread.  The AverageOn items take classes
+// 16..27: class 16 + c holds the AverageOn items of store class c < 12.  Each class kernel carries
+// both engines of its N and one mode.
+constexpr int kBatchClasses = 28;
+constexpr int kAvgClass0 = 16;
+__host__ __device__ constexpr int class_n(int c) { return c >= kAvgClass0 ? (c - kAvgClass0 < 9 ? c - kAvgClass0 + 2 : c - kAvgClass0 - 5) : (c < 9 ? c + 2 : c - 5); }
+__host__ __device__ constexpr bool class_ff(int c) { return (c >= 9 && c < 12) || (c >= kAvgClass0 + 9 && c < kAvgClass0 + 12); }
+__host__ __device__ constexpr bool class_split(int c) { return c >= 12 && c < kAvgClass0; }
+__host__ __device__ constexpr bool class_avg(int c) { return c >= kAvgClass0; }
 constexpr int kSplitMinN = 7;
 inline bool ff_class_n(int N) { return N >= f32::kHardMinN && N < f32::kPreciseN; }
-inline int batch_class(int N, bool ff, bool split = false)
+inline int batch_class(int N, bool ff, int mode, bool split = false)
 {
-    if (N < 2) return 0;
-    if (N > 10) return 8;
-    if (split && N >= kSplitMinN) return N + 5;
-    return (ff && ff_class_n(N)) ? N + 5 : N - 2;
+    const int base = N < 2 ? 0 : N > 10 ? 8 : (ff && ff_class_n(N)) ? N + 5 : N - 2;
+    if (mode == HPS_MODE_AVERAGE) return kAvgClass0 + base;
+    if (split && N >= kSplitMinN && N <= 10) return N + 5;
+    return base;
 }
 // The engine field of a table entry: the engine, with kPreciseForm for the float-float classes.
 inline int item_engine(int N, int engine, bool ff) { return engine | ((ff && ff_class_n(N)) ? kPreciseForm : 0); }
@@ -80,11 +81,19 @@ struct BatchHeader {
     int32_t store_tile;
 };
 
-template <int N, int ENGINE, bool SPLIT = false>
+// One work unit of an item.  MODE_ONLY >= 0 compiles the path of that mode alone (the per-class
+// kernels); -1 compiles both and dispatches on the item (the single kernel over every N).
+template <int N, int ENGINE, bool SPLIT = false, int MODE_ONLY = -1>
 __device__ __forceinline__ void run_unit(const BatchItemDev& it, uint64_t u, int store_tile, hps_stats* partials,
                                          void* smem)
 {
-    if (it.mode == HPS_MODE_STORE) {
+    if (MODE_ONLY == HPS_MODE_AVERAGE || (MODE_ONLY < 0 && it.mode != HPS_MODE_STORE)) {
+        if constexpr (!SPLIT && MODE_ONLY != HPS_MODE_STORE) {
+            const float K0 = *reinterpret_cast<const float*>(it.stats);      // written by k_batch_shift
+            const hps_sums r = average_tile_f32<N, ENGINE>(it.chd, it.chf, it.fn, it.first, it.n, u, K0, smem);
+            if (threadIdx.x == 0) reinterpret_cast<hps_sums*>(partials)[it.partial_offset + u] = r;
+        }
+    } else if constexpr (MODE_ONLY != HPS_MODE_AVERAGE) {
         const uint64_t lo = u * (uint64_t)store_tile;
         const uint64_t hi = (lo + store_tile < it.n) ? lo + store_tile : it.n;
         // the unit fetch ends with a __syncthreads, so each unit may start at parity 0
@@ -98,10 +107,6 @@ __device__ __forceinline__ void run_unit(const BatchItemDev& it, uint64_t u, int
                 store_chunk_f32<N, ENGINE>(it.chd, it.chf, it.cols, it.weights, it.flags, it.ukey, it.first, hi, cb,
                                            it.vec32 != 0, smem, parity);
         }
-    } else if constexpr (!SPLIT) {
-        const float K0 = *reinterpret_cast<const float*>(it.stats);      // written by k_batch_shift
-        const hps_sums r = average_tile_f32<N, ENGINE>(it.chd, it.chf, it.fn, it.first, it.n, u, K0, smem);
-        if (threadIdx.x == 0) reinterpret_cast<hps_sums*>(partials)[it.partial_offset + u] = r;
     }
 }
 
@@ -146,23 +151,25 @@ __device__ __forceinline__ void batch_body(const BatchItemDev* __restrict__ item
         __syncthreads();                                  // s_it staged; s_unit / s_item read before they change
         const BatchItemDev& it = s_it;
         const uint64_t lu = u - it.unit_begin;
+        constexpr int MODE = class_avg(CLS) ? HPS_MODE_AVERAGE : HPS_MODE_STORE;
+        constexpr bool SPL = class_split(CLS);
         switch (it.N * 8 + it.engine) {
 #define HPS_UNIT(NN)                                                                             \
         case NN * 8 + 0:                                                                         \
             if constexpr (NN == class_n(CLS) && !class_ff(CLS))                                  \
-                run_unit<NN, kPhilox, class_split(CLS)>(it, lu, store_tile, partials, smem);     \
+                run_unit<NN, kPhilox, SPL, MODE>(it, lu, store_tile, partials, smem);            \
             break;                                                                               \
         case NN * 8 + 1:                                                                         \
             if constexpr (NN == class_n(CLS) && !class_ff(CLS))                                  \
-                run_unit<NN, kSquares3, class_split(CLS)>(it, lu, store_tile, partials, smem);   \
+                run_unit<NN, kSquares3, SPL, MODE>(it, lu, store_tile, partials, smem);          \
             break;                                                                               \
         case NN * 8 + kPreciseForm:                                                              \
             if constexpr (NN == class_n(CLS) && class_ff(CLS))                                   \
-                run_unit<NN, kPhilox | kPreciseForm>(it, lu, store_tile, partials, smem);        \
+                run_unit<NN, kPhilox | kPreciseForm, false, MODE>(it, lu, store_tile, partials, smem);   \
             break;                                                                               \
         case NN * 8 + (kSquares3 | kPreciseForm):                                                \
             if constexpr (NN == class_n(CLS) && class_ff(CLS))                                   \
-                run_unit<NN, kSquares3 | kPreciseForm>(it, lu, store_tile, partials, smem);      \
+                run_unit<NN, kSquares3 | kPreciseForm, false, MODE>(it, lu, store_tile, partials, smem); \
             break;
         HPS_UNIT(2) HPS_UNIT(3) HPS_UNIT(4) HPS_UNIT(5) HPS_UNIT(6) HPS_UNIT(7) HPS_UNIT(8) HPS_UNIT(9)
         HPS_UNIT(10)
@@ -173,10 +180,13 @@ __device__ __forceinline__ void batch_body(const BatchItemDev* __restrict__ item
 }
 
 // Resident CTAs per SM the register allocation of a class kernel must allow (second argument of
-// __launch_bounds__; 0 leaves the choice to the compiler).  The N >= 7 classes held to 128
-// registers (2 CTAs per SM) took the 256-channel batch from 2.776 ms to 2.612 ms (best of the
-// autotuner's CTAs per SM each); capping from N = 8 or only N = 10 gave 2.616 and 2.635 ms, and
-// 80 registers spill 360 to 1448 bytes.
+// __launch_bounds__; 0 leaves the choice to the compiler).  The classes of N >= 7 (both modes) are
+// held to 128 registers (2 CTAs per SM).  Measured on the 256-channel batch (autotuned, ms; store
+// only / every other channel an AverageOn item): one kernel per N for both modes 2.564 / 2.700;
+// one per N and mode with the store classes at the single-channel store kernel's bounds (64, 80,
+// 80, 128 registers for N = 7..10; they spill 144 to 248 bytes here) 2.558 / 2.537; one per N and
+// mode at 128 registers 2.537 / 2.516.  When one kernel carried both modes, holding N >= 7 to 128
+// registers had taken the batch from 2.776 to 2.612 ms.
 __host__ __device__ constexpr int batch_min_ctas(int c) { return (!class_split(c) && class_n(c) >= 7) ? 2 : 0; }
 
 template <int CLS>
@@ -290,12 +300,12 @@ typedef void (*BatchKernel)(const BatchItemDev*, BatchHeader*, hps_stats*);
 
 inline BatchKernel class_kernel(int c)
 {
-    static const BatchKernel k[kBatchClasses] = {k_batch_f32<0>, k_batch_f32<1>, k_batch_f32<2>,
-                                                 k_batch_f32<3>, k_batch_f32<4>, k_batch_f32<5>,
-                                                 k_batch_f32<6>, k_batch_f32<7>, k_batch_f32<8>,
-                                                 k_batch_f32<9>, k_batch_f32<10>, k_batch_f32<11>,
-                                                 k_batch_f32<12>, k_batch_f32<13>, k_batch_f32<14>,
-                                                 k_batch_f32<15>};
+    static const BatchKernel k[kBatchClasses] = {
+        k_batch_f32<0>,  k_batch_f32<1>,  k_batch_f32<2>,  k_batch_f32<3>,  k_batch_f32<4>,  k_batch_f32<5>,
+        k_batch_f32<6>,  k_batch_f32<7>,  k_batch_f32<8>,  k_batch_f32<9>,  k_batch_f32<10>, k_batch_f32<11>,
+        k_batch_f32<12>, k_batch_f32<13>, k_batch_f32<14>, k_batch_f32<15>, k_batch_f32<16>, k_batch_f32<17>,
+        k_batch_f32<18>, k_batch_f32<19>, k_batch_f32<20>, k_batch_f32<21>, k_batch_f32<22>, k_batch_f32<23>,
+        k_batch_f32<24>, k_batch_f32<25>, k_batch_f32<26>, k_batch_f32<27>};
     return k[c];
 }
 
@@ -321,11 +331,13 @@ struct hps_batch_plan {
     std::vector<hps_batch_item> items;  // host copy, re-cut when the store tile changes
     uint64_t total_events = 0;
     std::vector<int> mix;              // item mix signature for the tuning cache
-    cudaStream_t capture = nullptr;
-    cudaStream_t branch[kBatchClasses] = {};     // capture streams of the class kernels
-    cudaEvent_t fork = nullptr, join[kBatchClasses] = {};
+    cudaStream_t own = nullptr;                  // the plan's stream for re-cutting the table
     int occupancy[kBatchClasses + 1] = {};       // resident CTAs per SM of each class kernel, then of
                                                  // the single kernel over every N
+    uint64_t class_units[kBatchClasses] = {};    // work units of each class in the current table
+    unsigned class_grid_set[kBatchClasses] = {};  // grid of each class kernel node in exec
+    cudaGraph_t graph = nullptr;                 // kept while exec lives: its class kernel nodes are
+    cudaGraphNode_t class_node[kBatchClasses] = {};   // re-gridded when the table changes
     cudaGraphExec_t exec = nullptr;
 };
 
@@ -333,50 +345,122 @@ namespace {
 
 hps_status destroy_graph(hps_batch_plan* p)
 {
+    cudaError_t e = cudaSuccess;
     if (p->exec) {
-        cudaError_t e = cudaGraphExecDestroy(p->exec);
+        e = cudaGraphExecDestroy(p->exec);
         p->exec = nullptr;
-        if (e != cudaSuccess) return cuda_status(e, "cudaGraphExecDestroy");
+    }
+    if (p->graph) {
+        const cudaError_t e2 = cudaGraphDestroy(p->graph);
+        p->graph = nullptr;
+        if (e == cudaSuccess) e = e2;
+    }
+    for (int c = 0; c < kBatchClasses; ++c) p->class_node[c] = nullptr;
+    return e == cudaSuccess ? HPS_OK : cuda_status(e, "destroy batch graph");
+}
+
+// Grid of class kernel c: the tuning's CTAs per SM within the kernel's occupancy, no more CTAs than
+// the class has units (each CTA takes units from the class counter), and one CTA for an empty class.
+unsigned class_grid(const hps_batch_plan* p, int c)
+{
+    const int ctas = p->tuning.ctas_per_sm < p->occupancy[c] ? p->tuning.ctas_per_sm : p->occupancy[c];
+    const uint64_t full = static_cast<uint64_t>(ctas > 0 ? ctas : 1) * static_cast<uint64_t>(p->sm_count);
+    const uint64_t units = p->class_units[c];
+    return static_cast<unsigned>(units == 0 ? 1 : units < full ? units : full);
+}
+
+// Kernel node parameters of one launch of the plan's kernels (all take items, header, partials).
+cudaKernelNodeParams kernel_params(void* func, unsigned grid, unsigned block, void** args)
+{
+    cudaKernelNodeParams kp;
+    std::memset(&kp, 0, sizeof(kp));
+    kp.func = func;
+    kp.gridDim = dim3(grid, 1, 1);
+    kp.blockDim = dim3(block, 1, 1);
+    kp.sharedMemBytes = 0;
+    kp.kernelParams = args;
+    kp.extra = nullptr;
+    return kp;
+}
+
+// Sets the grid of each class kernel node of the instantiated graph whose unit count changed the
+// grid (takes effect from the next launch; a launch in flight keeps its grids).  A graph of the
+// single kernel over every N has no class nodes; a change of kernel form builds a new graph.
+hps_status apply_class_grids(hps_batch_plan* p)
+{
+    if (!p->exec) return HPS_OK;
+    for (int c = 0; c < kBatchClasses; ++c) {
+        if (!p->class_node[c]) continue;
+        const unsigned g = class_grid(p, c);
+        if (g == p->class_grid_set[c]) continue;
+        void* args[3] = {&p->d_items, &p->d_header, &p->d_partials};
+        const cudaKernelNodeParams kp = kernel_params(reinterpret_cast<void*>(class_kernel(c)), g, kTileThreads, args);
+        const cudaError_t e = cudaGraphExecKernelNodeSetParams(p->exec, p->class_node[c], &kp);
+        if (e != cudaSuccess) return cuda_status(e, "cudaGraphExecKernelNodeSetParams");
+        p->class_grid_set[c] = g;
     }
     return HPS_OK;
 }
 
+// The graph, built node by node: counter reset -> K0 shifts -> the class kernels (parallel
+// branches) or the single kernel -> per-item merge.
 hps_status build_graph(hps_batch_plan* p)
 {
     hps_status st = destroy_graph(p);
     if (st != HPS_OK) return st;
+    void* args[3] = {&p->d_items, &p->d_header, &p->d_partials};
     cudaGraph_t graph = nullptr;
-    cudaError_t e = cudaStreamBeginCapture(p->capture, cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess) return cuda_status(e, "cudaStreamBeginCapture");
-    cudaMemsetAsync(p->d_header->counter, 0, sizeof(p->d_header->counter), p->capture);
-    k_batch_shift<<<static_cast<unsigned>(p->max_items), 32, 0, p->capture>>>(p->d_items, p->d_header);
-    auto grid_of = [p](int c) {
-        const int ctas = p->tuning.ctas_per_sm < p->occupancy[c] ? p->tuning.ctas_per_sm : p->occupancy[c];
-        return static_cast<unsigned>((ctas > 0 ? ctas : 1) * p->sm_count);
-    };
-    if (p->tuning.kernel_form == HPS_BATCH_ONE_KERNEL) {
-        k_batch_f32_all<<<grid_of(kBatchClasses), kTileThreads, 0, p->capture>>>(p->d_items, p->d_header,
-                                                                                 p->d_partials);
-    } else {
-        // the class kernels as parallel branches between a fork and a join
-        cudaEventRecord(p->fork, p->capture);
-        for (int c = 0; c < kBatchClasses; ++c) {
-            cudaStreamWaitEvent(p->branch[c], p->fork, 0);
-            class_kernel(c)<<<grid_of(c), kTileThreads, 0, p->branch[c]>>>(p->d_items, p->d_header, p->d_partials);
-            cudaEventRecord(p->join[c], p->branch[c]);
-            cudaStreamWaitEvent(p->capture, p->join[c], 0);
+    cudaError_t e = cudaGraphCreate(&graph, 0);
+    if (e != cudaSuccess) return cuda_status(e, "cudaGraphCreate");
+    cudaGraphNode_t reset = nullptr, shift = nullptr, merge = nullptr;
+    std::vector<cudaGraphNode_t> work;
+    {
+        cudaMemsetParams mp;
+        std::memset(&mp, 0, sizeof(mp));
+        mp.dst = p->d_header->counter;
+        mp.value = 0;
+        mp.elementSize = 4;
+        mp.width = sizeof(p->d_header->counter) / 4;
+        mp.height = 1;
+        mp.pitch = 0;
+        e = cudaGraphAddMemsetNode(&reset, graph, nullptr, 0, &mp);
+    }
+    if (e == cudaSuccess) {
+        const cudaKernelNodeParams kp =
+            kernel_params(reinterpret_cast<void*>(k_batch_shift), static_cast<unsigned>(p->max_items), 32, args);
+        e = cudaGraphAddKernelNode(&shift, graph, &reset, 1, &kp);
+    }
+    if (e == cudaSuccess && p->tuning.kernel_form == HPS_BATCH_ONE_KERNEL) {
+        const int ctas = p->tuning.ctas_per_sm < p->occupancy[kBatchClasses] ? p->tuning.ctas_per_sm
+                                                                              : p->occupancy[kBatchClasses];
+        const cudaKernelNodeParams kp = kernel_params(reinterpret_cast<void*>(k_batch_f32_all),
+                                                      static_cast<unsigned>((ctas > 0 ? ctas : 1) * p->sm_count),
+                                                      kTileThreads, args);
+        cudaGraphNode_t n = nullptr;
+        e = cudaGraphAddKernelNode(&n, graph, &shift, 1, &kp);
+        work.push_back(n);
+    } else if (e == cudaSuccess) {
+        for (int c = 0; c < kBatchClasses && e == cudaSuccess; ++c) {
+            p->class_grid_set[c] = class_grid(p, c);
+            const cudaKernelNodeParams kp =
+                kernel_params(reinterpret_cast<void*>(class_kernel(c)), p->class_grid_set[c], kTileThreads, args);
+            e = cudaGraphAddKernelNode(&p->class_node[c], graph, &shift, 1, &kp);
+            work.push_back(p->class_node[c]);
         }
     }
-    k_batch_merge<<<static_cast<unsigned>(p->max_items), kFinalThreads, 0, p->capture>>>(p->d_items, p->d_header,
-                                                                                         p->d_partials);
-    e = cudaStreamEndCapture(p->capture, &graph);
-    if (e != cudaSuccess) return cuda_status(e, "cudaStreamEndCapture");
-    e = cudaGraphInstantiate(&p->exec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (e != cudaSuccess) {
-        p->exec = nullptr;
-        return cuda_status(e, "cudaGraphInstantiate");
+    if (e == cudaSuccess) {
+        const cudaKernelNodeParams kp = kernel_params(reinterpret_cast<void*>(k_batch_merge),
+                                                      static_cast<unsigned>(p->max_items), kFinalThreads, args);
+        e = cudaGraphAddKernelNode(&merge, graph, work.data(), work.size(), &kp);
     }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&p->exec, graph, 0);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        for (int c = 0; c < kBatchClasses; ++c) p->class_node[c] = nullptr;
+        p->exec = nullptr;
+        return cuda_status(e, "batch graph");
+    }
+    p->graph = graph;
     return HPS_OK;
 }
 
@@ -438,7 +522,7 @@ hps_status upload_items(hps_batch_plan* p, const std::vector<hps_batch_item>& it
     int32_t item_begin[kBatchClasses + 1] = {};
     const bool split = p->tuning.threads_per_event == 2;
     auto cls = [&](int i) {
-        return batch_class(items[i].channel.n_daughters, float_float_form(&items[i].channel),
+        return batch_class(items[i].channel.n_daughters, float_float_form(&items[i].channel), items[i].mode,
                            split && items[i].mode == HPS_MODE_STORE);
     };
     for (int i = 0; i < n_items; ++i) ++item_begin[cls(i) + 1];
@@ -509,6 +593,7 @@ hps_status upload_items(hps_batch_plan* p, const std::vector<hps_batch_item>& it
         p->h_header->class_begin[c] = class_begin[c];
         p->h_header->item_begin[c] = item_begin[c];
     }
+    for (int c = 0; c < kBatchClasses; ++c) p->class_units[c] = class_begin[c + 1] - class_begin[c];
     p->h_header->n_items = n_items;
     p->h_header->store_tile = p->tuning.store_tile_events;
     p->n_items = n_items;
@@ -521,7 +606,7 @@ hps_status upload_items(hps_batch_plan* p, const std::vector<hps_batch_item>& it
     if (e == cudaSuccess) e = cudaEventRecord(p->staged, s);
     if (e != cudaSuccess) return cuda_status(e, "batch table upload");
     p->staged_pending = true;
-    return HPS_OK;
+    return apply_class_grids(p);
 }
 
 }  // namespace
@@ -554,12 +639,7 @@ hps_status hps_batch_create(hps_batch_plan** out, int32_t max_items, uint64_t ma
     if (e == cudaSuccess) e = cudaMallocHost(&p->h_items, sizeof(BatchItemDev) * max_items);
     if (e == cudaSuccess) e = cudaMallocHost(&p->h_header, sizeof(BatchHeader));
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->staged, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->capture, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming);
-    for (int c = 0; c < kBatchClasses && e == cudaSuccess; ++c) {
-        e = cudaStreamCreateWithFlags(&p->branch[c], cudaStreamNonBlocking);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->join[c], cudaEventDisableTiming);
-    }
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->own, cudaStreamNonBlocking);
     for (int c = 0; c < kBatchClasses && e == cudaSuccess; ++c)
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p->occupancy[c], class_kernel(c), kTileThreads, 0);
     if (e == cudaSuccess)
@@ -625,9 +705,9 @@ hps_status hps_batch_set_tuning(hps_batch_plan* p, const hps_batch_tuning* t)
     p->tuning = *t;
     if (tile_changed && p->n_items > 0) {
         // re-cut the current items into the new store tile; done on the plan's own stream
-        st = upload_items(p, p->items, p->capture);
+        st = upload_items(p, p->items, p->own);
         if (st != HPS_OK) return st;
-        cudaError_t e = cudaStreamSynchronize(p->capture);
+        cudaError_t e = cudaStreamSynchronize(p->own);
         if (e != cudaSuccess) return cuda_status(e, "cudaStreamSynchronize");
     }
     return build_graph(p);
@@ -710,12 +790,7 @@ hps_status hps_batch_destroy(hps_batch_plan* p)
     if (!p) return HPS_OK;
     destroy_graph(p);
     if (p->staged) { cudaEventSynchronize(p->staged); cudaEventDestroy(p->staged); }
-    if (p->capture) cudaStreamDestroy(p->capture);
-    if (p->fork) cudaEventDestroy(p->fork);
-    for (int c = 0; c < kBatchClasses; ++c) {
-        if (p->branch[c]) cudaStreamDestroy(p->branch[c]);
-        if (p->join[c]) cudaEventDestroy(p->join[c]);
-    }
+    if (p->own) cudaStreamDestroy(p->own);
     if (p->d_items) cudaFree(p->d_items);
     if (p->d_header) cudaFree(p->d_header);
     if (p->d_partials) cudaFree(p->d_partials);

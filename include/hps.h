@@ -343,8 +343,8 @@ hps_status hps_rng_words(int32_t n_daughters, int32_t engine, uint64_t seed, uin
 /* ------------------------------------------------------ batched channels, one graph launch -- */
 
 /* Many decay channels of different N and event counts in one graph launch of persistent kernels
- * (FP32_FIX arithmetic): one per N, so that each runs at the occupancy of its own register count,
- * or one over every N (hps_batch_tuning.kernel_form; the autotuner tries both).  There is no
+ * (FP32_FIX arithmetic): one per N and mode, so that each runs at the occupancy of its own
+ * register count, or one over every N (hps_batch_tuning.kernel_form; the autotuner tries both).  There is no
  * single reference call for this: it batches what would be one PhaseSpace::Generate or AverageOn
  * call per channel (PhaseSpace.inl:255-444).  Each item's
  * results are bit-identical to the same request made alone with hps_generate / hps_average_on
@@ -368,8 +368,9 @@ typedef struct hps_batch_item {
 /* Launch shape of the persistent kernels: each gets min(ctas_per_sm, the CTAs of it that fit
  * on an SM) x SM count CTAs of 256 threads; store items are cut into work units of
  * store_tile_events events (a multiple of 256), AverageOn items into tiles of HPS_AVG_TILE events.
- * kernel_form: HPS_BATCH_PER_N runs one persistent kernel per N as parallel branches of the
- * graph, each at the occupancy of its own register count; HPS_BATCH_ONE_KERNEL runs one
+ * kernel_form: HPS_BATCH_PER_N runs one persistent kernel per N and mode as parallel branches of
+ * the graph, each at the occupancy of its own register count and with no more CTAs than its work
+ * units; HPS_BATCH_ONE_KERNEL runs one
  * persistent kernel over every N (the register count of N = 10 for all).  threads_per_event: 1,
  * each thread owns one event (its kinematics stay in that thread's registers; the random words
  * of a CTA's events are computed cooperatively); 2 (per-N form only), each store event with
