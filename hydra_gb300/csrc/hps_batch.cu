@@ -181,13 +181,19 @@ __device__ __forceinline__ void batch_body(const BatchItemDev* __restrict__ item
 
 // Resident CTAs per SM the register allocation of a class kernel must allow (second argument of
 // __launch_bounds__; 0 leaves the choice to the compiler).  The classes of N >= 7 (both modes) are
-// held to 128 registers (2 CTAs per SM).  Measured on the 256-channel batch (autotuned, ms; store
-// only / every other channel an AverageOn item): one kernel per N for both modes 2.564 / 2.700;
-// one per N and mode with the store classes at the single-channel store kernel's bounds (64, 80,
-// 80, 128 registers for N = 7..10; they spill 144 to 248 bytes here) 2.558 / 2.537; one per N and
-// mode at 128 registers 2.537 / 2.516.  When one kernel carried both modes, holding N >= 7 to 128
-// registers had taken the batch from 2.776 to 2.612 ms.
-__host__ __device__ constexpr int batch_min_ctas(int c) { return (!class_split(c) && class_n(c) >= 7) ? 2 : 0; }
+// held to 128 registers (2 CTAs per SM), the store classes of N <= 6 to 64 (4 CTAs per SM; the
+// compiler gives them up to 98: the unit loop and the staged item add to the event body's).
+// Measured on the 256-channel batch (autotuned, ms; store only / every other channel an AverageOn
+// item): one kernel per N for both modes 2.564 / 2.700; one per N and mode with the store classes
+// of N >= 7 at the single-channel store kernel's bounds (64, 80, 80, 128 registers for N = 7..10;
+// they spill 144 to 248 bytes here) 2.558 / 2.537; one per N and mode at 128 registers for N >= 7
+// 2.537 / 2.516; and with the store classes of N <= 6 at 64 registers 2.486 / 2.494 (at 48
+// registers, spilling up to 112 bytes, 2.517 / 2.522).  When one kernel carried both modes,
+// holding N >= 7 to 128 registers had taken the batch from 2.776 to 2.612 ms.
+__host__ __device__ constexpr int batch_min_ctas(int c)
+{
+    return (!class_split(c) && class_n(c) >= 7) ? 2 : (!class_avg(c) && !class_split(c)) ? 4 : 0;
+}
 
 template <int CLS>
 __global__ void __launch_bounds__(kTileThreads, batch_min_ctas(CLS))
