@@ -81,8 +81,16 @@ struct BatchHeader {
     int32_t store_tile;
 };
 
+// Store loop of the per-class kernels: two events per thread, one after the other, from one
+// exchange of the random words of two chunks (store_pair_seq_f32), except for N = 8 and 9, which
+// take one chunk per exchange, as the single-channel store kernel does.  On the 256-channel batch
+// (ms, store only / mixed): one chunk per exchange for every N 2.488 / 2.494; the single-channel
+// kernel's forms (N <= 4 with the two events interleaved) 2.454 / 2.484; this 2.441 / 2.473.
+__host__ __device__ constexpr bool batch_store_paired(int N) { return N != 8 && N != 9; }
+
 // One work unit of an item.  MODE_ONLY >= 0 compiles the path of that mode alone (the per-class
-// kernels); -1 compiles both and dispatches on the item (the single kernel over every N).
+// kernels); -1 compiles both and dispatches on the item (the single kernel over every N, whose
+// store loop takes one chunk per exchange).
 template <int N, int ENGINE, bool SPLIT = false, int MODE_ONLY = -1>
 __device__ __forceinline__ void run_unit(const BatchItemDev& it, uint64_t u, int store_tile, hps_stats* partials,
                                          void* smem)
@@ -102,6 +110,10 @@ __device__ __forceinline__ void run_unit(const BatchItemDev& it, uint64_t u, int
             for (uint64_t cb = lo; cb < hi; cb += kTileThreads / 2, parity ^= 1)
                 store_chunk_split_f32<N, ENGINE>(it.chd, it.chf, it.cols, it.weights, it.flags, it.ukey, it.first, hi,
                                                  cb, it.vec32 != 0, smem, parity);
+        } else if constexpr (MODE_ONLY == HPS_MODE_STORE && batch_store_paired(N)) {
+            for (uint64_t cb = lo; cb < hi; cb += 2 * kTileThreads, parity ^= 1)
+                store_pair_seq_f32<N, ENGINE, kTileThreads>(it.chd, it.chf, it.cols, it.weights, it.flags, it.ukey,
+                                                            it.first, hi, cb, it.vec32 != 0, smem, parity);
         } else {
             for (uint64_t cb = lo; cb < hi; cb += kTileThreads, parity ^= 1)
                 store_chunk_f32<N, ENGINE>(it.chd, it.chf, it.cols, it.weights, it.flags, it.ukey, it.first, hi, cb,
@@ -114,8 +126,11 @@ template <int CLS>
 __device__ __forceinline__ void batch_body(const BatchItemDev* __restrict__ items, BatchHeader* __restrict__ hdr,
                                            hps_stats* __restrict__ partials)
 {
-    // largest shared-memory word exchange of the class (Philox at its largest N)
-    __shared__ __align__(16) unsigned char smem[WordShare<class_n(CLS), kPhilox, kTileThreads>::BYTES2];
+    // largest shared-memory word exchange of the class (Philox; two chunks at a time in the paired
+    // store loops)
+    constexpr bool kPairedStore = !class_avg(CLS) && !class_split(CLS) && batch_store_paired(class_n(CLS));
+    __shared__ __align__(16) unsigned char
+        smem[kPairedStore ? PairedSmem<class_n(CLS), kPhilox>::BYTES : WordShare<class_n(CLS), kPhilox, kTileThreads>::BYTES2];
     __shared__ unsigned long long s_unit;
     __shared__ int s_item;
     // The unit's item, staged in shared memory: the channel constants are then re-read after the
