@@ -203,8 +203,11 @@ __device__ __forceinline__ void batch_body(const BatchItemDev* __restrict__ item
 // of N >= 7 at the single-channel store kernel's bounds (64, 80, 80, 128 registers for N = 7..10;
 // they spill 144 to 248 bytes here) 2.558 / 2.537; one per N and mode at 128 registers for N >= 7
 // 2.537 / 2.516; and with the store classes of N <= 6 at 64 registers 2.486 / 2.494 (at 48
-// registers, spilling up to 112 bytes, 2.517 / 2.522).  When one kernel carried both modes,
-// holding N >= 7 to 128 registers had taken the batch from 2.776 to 2.612 ms.
+// registers, spilling up to 112 bytes, 2.517 / 2.522).  The AverageOn classes of N <= 6 keep the
+// compiler's 59..80 registers: at 64 registers the mixed batch and an AverageOn-only batch of the
+// same channels measured 2.461 / 2.303 ms against 2.472 / 2.297, and 2.461 / 2.310 with paired
+// tiles for N = 3..5.  When one kernel carried both modes, holding N >= 7 to 128 registers had
+// taken the batch from 2.776 to 2.612 ms.
 __host__ __device__ constexpr int batch_min_ctas(int c)
 {
     return (!class_split(c) && class_n(c) >= 7) ? 2 : (!class_avg(c) && !class_split(c)) ? 4 : 0;
