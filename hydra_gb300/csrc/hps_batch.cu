@@ -55,8 +55,14 @@ struct BatchItemDev {
 // both engines of its N and one mode.
 constexpr int kBatchClasses = 28;
 constexpr int kAvgClass0 = 16;
-__host__ __device__ constexpr int class_n(int c) { return c >= kAvgClass0 ? (c - kAvgClass0 < 9 ? c - kAvgClass0 + 2 : c - kAvgClass0 - 5) : (c < 9 ? c + 2 : c - 5); }
-__host__ __device__ constexpr bool class_ff(int c) { return (c >= 9 && c < 12) || (c >= kAvgClass0 + 9 && c < kAvgClass0 + 12); }
+__host__ __device__ constexpr int class_n(int c)
+{
+    return c >= kAvgClass0 ? class_n(c - kAvgClass0) : c < 9 ? c + 2 : c - 5;
+}
+__host__ __device__ constexpr bool class_ff(int c)
+{
+    return c >= kAvgClass0 ? class_ff(c - kAvgClass0) : (c >= 9 && c < 12);
+}
 __host__ __device__ constexpr bool class_split(int c) { return c >= 12 && c < kAvgClass0; }
 __host__ __device__ constexpr bool class_avg(int c) { return c >= kAvgClass0; }
 constexpr int kSplitMinN = 7;
