@@ -773,7 +773,10 @@ hps_status hps_batch_autotune(hps_batch_plan* p, void* stream, const char* cache
     cudaEventCreate(&a);
     cudaEventCreate(&b);
     const int ctas[] = {1, 2, 3, 4, 6, 8};
-    const int tiles[] = {4096, 16384, 65536};
+    // 2048-event units pay where AverageOn items share the launch (the 256-channel batch with every
+    // other channel an AverageOn item: 2.472 ms against 2.482 at 4096); store-only mixes keep 4096
+    // (2.450 against 2.441), and 1024 is slower for both (2.497, 2.495)
+    const int tiles[] = {2048, 4096, 16384, 65536};
     // threads per event 2 only where there are store items it applies to (N >= 7)
     bool any_split = false;
     for (const hps_batch_item& it : p->items)
