@@ -183,8 +183,9 @@ def test_batch_rejects_bad_item(api, torch, hps):
 
 
 def test_batch_single_class_empty_and_reordered(api, torch):
-    """Items of one N only (the other per-N kernels find no work), an empty item list, and a
-    mix given in descending N (the table is reordered by N): every item equals its call alone."""
+    """Items of one N only (the other class kernels find no work and launch one CTA each), an
+    empty item list, and a mix given in descending N (the table is reordered by N), on one plan
+    whose class kernel grids follow each new table: every item equals its call alone."""
     mix = [r for r in make_mix(api, torch, 60, seed=4) if r[1].n_daughters == 5][:4]
     assert mix
     plan = api.BatchPlan(32, 512)
