@@ -5,7 +5,9 @@
 // the precision contract of the float body on channels and event counts beyond the GPU tests
 // (tests/test_f32_emulation.py; build with tests/f32_emulation/build.sh).
 //
-//   emulate_f32 N M m0,m1,... n_events [first] [engine 0 philox | 1 squares3] [seed]
+//   emulate_f32 N M m0,m1,... n_events [first] [engine 0 philox | 1 squares3] [seed] [form]
+// form -1 (default): the library's choice for the channel; 0: the plain form; 1: the float-float
+// boosts (N = 4..6; from N = 7 the full form is taken whatever is asked).
 #include "cuda_shim.h"
 #include "hydra_gb300/csrc/genbod_f32.cuh"
 
@@ -111,6 +113,7 @@ int main(int argc, char** argv)
     make_channel(c, ch);
     DevChannelF chf;
     f32::make_channel_f(c, chf);
+    if (argc > 8 && std::atoi(argv[8]) >= 0) chf.precise = std::atoi(argv[8]) ? 1 : 0;
     Worst r;
     switch (N) {
     case 2: r = dispatch<2>(ch, chf, first, n, engine); break;

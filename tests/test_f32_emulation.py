@@ -34,8 +34,9 @@ def emulator():
     return r.stdout.strip().splitlines()[-1]
 
 
-def run(exe, masses, M, n, first=0, engine=0):
-    args = [exe, str(len(masses)), repr(M), ",".join(repr(m) for m in masses), str(n), str(first), str(engine)]
+def run(exe, masses, M, n, first=0, engine=0, form=-1):
+    args = [exe, str(len(masses)), repr(M), ",".join(repr(m) for m in masses), str(n), str(first), str(engine),
+            "0x3039", str(form)]
     r = subprocess.run(args, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr
     return json.loads(r.stdout)
@@ -66,3 +67,15 @@ def test_emulated_weight_product_range(emulator):
     normal range before each stage took an even power of two out of it (85% weight error)."""
     d = run(emulator, [PI] * 10, 8.0, 128, first=13901700)
     assert d["weights"] <= TOL and d["four_vectors"] <= TOL, d
+
+
+def test_emulated_forms_of_a_hard_channel(emulator):
+    """Six pions from 3 GeV (kinetic energy 15.5 pion masses, above the float-float boosts'
+    threshold of 12): the library takes the float-float boosts; the plain form of the same events
+    is within the contract too, with less margin."""
+    masses, M = [PI] * 6, 3.0
+    auto = run(emulator, masses, M, 1 << 18)
+    plain = run(emulator, masses, M, 1 << 18, form=0)
+    assert auto["float_float_form"] == 1 and plain["float_float_form"] == 0
+    assert auto["four_vectors"] <= plain["four_vectors"] <= TOL, (auto, plain)
+    assert auto["weights"] <= TOL and plain["weights"] <= TOL
