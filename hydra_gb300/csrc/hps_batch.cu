@@ -415,7 +415,9 @@ cudaKernelNodeParams kernel_params(void* func, unsigned grid, unsigned block, vo
 
 // Sets the grid of each class kernel node of the instantiated graph whose unit count changed the
 // grid (takes effect from the next launch; a launch in flight keeps its grids).  A graph of the
-// single kernel over every N has no class nodes; a change of kernel form builds a new graph.
+// single kernel over every N has no class nodes; a change of kernel form builds a new graph.  The
+// grids shape the launch only: the CTAs of a class loop on its unit counter, so any grid of one
+// CTA or more covers every unit, and a failed update leaves a correct (if slower) graph.
 hps_status apply_class_grids(hps_batch_plan* p)
 {
     if (!p->exec) return HPS_OK;
