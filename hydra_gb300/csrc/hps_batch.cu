@@ -91,7 +91,9 @@ struct BatchHeader {
 // exchange of the random words of two chunks (store_pair_seq_f32), except for N = 8 and 9, which
 // take one chunk per exchange, as the single-channel store kernel does.  On the 256-channel batch
 // (ms, store only / mixed): one chunk per exchange for every N 2.488 / 2.494; the single-channel
-// kernel's forms (N <= 4 with the two events interleaved) 2.454 / 2.484; this 2.441 / 2.473.
+// kernel's forms (N <= 4 with the two events interleaved) 2.454 / 2.484; this 2.441 / 2.473.  The
+// single-channel kernel's 128-thread CTAs for N <= 6 (8 per SM at 64 registers) measured 2.443 /
+// 2.478 against 2.442 / 2.467 with 256, so every class runs 256-thread CTAs.
 __host__ __device__ constexpr bool batch_store_paired(int N) { return N != 8 && N != 9; }
 
 // One work unit of an item.  MODE_ONLY >= 0 compiles the path of that mode alone (the per-class
