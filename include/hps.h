@@ -394,7 +394,8 @@ typedef struct hps_batch_plan hps_batch_plan;
  * CUDA graph (counter reset, the persistent kernel(s), per-item merge).  tuning = NULL picks the default shape; hps_batch_autotune chooses one by timing. */
 hps_status hps_batch_create(hps_batch_plan** plan, int32_t max_items, uint64_t max_average_tiles,
                             int32_t precision, const hps_batch_tuning* tuning);
-/* Validates the items and uploads the table asynchronously on `stream`. */
+/* Validates the items and uploads the table asynchronously on `stream`; sets each class kernel's
+ * grid in the plan's graph to at most its number of work units (from the next launch; no new graph). */
 hps_status hps_batch_set_items(hps_batch_plan* plan, const hps_batch_item* items, int32_t n_items,
                                void* stream);
 /* One graph launch over the current items, asynchronous on `stream`. */
